@@ -1,0 +1,134 @@
+/*
+ * mpsim_gb300.h -- C ABI of the GB300 (sm_103a) MPS gate-application core.
+ *
+ * All tensor pointers are DEVICE pointers to interleaved complex64 (two
+ * floats, the layout of numpy.complex64 / torch.complex64).  Every call takes
+ * an explicit cudaStream_t (passed as void*) and enqueues its kernels on it.
+ * Functions return MPS_OK (0) or a nonzero MPS_ERR_* code; mps_last_error()
+ * gives a message for the most recent failure on the calling thread.
+ *
+ * Site tensors use the layout (chi_left, d, chi_right), row-major: element
+ * (l, a, r) at ((l * d) + a) * chi_right + r.  A gate acting on one qudit is a
+ * d x d matrix U[a', a]; a gate acting on two qudits is a (d*d) x (d*d)
+ * matrix G[(a' b'), (a b)] where a is the qudit of the LEFT site.
+ *
+ * The reference (grmlarose/mpsim) is pure Python and has no native
+ * interface; each entry point names the Python method of mpsim/core.py whose
+ * arithmetic it replaces.  The Python package mpsim_gb300 binds these through
+ * ctypes and keeps mpsim's method names and error behaviour.
+ */
+#ifndef MPSIM_GB300_H
+#define MPSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPS_OK 0
+#define MPS_ERR_ARG 1          /* invalid argument (shape, pointer, size)   */
+#define MPS_ERR_CUDA 2         /* a CUDA runtime call failed                */
+#define MPS_ERR_WORKSPACE 3    /* workspace too small                       */
+#define MPS_ERR_NOT_CONVERGED 4/* Jacobi SVD hit its sweep cap              */
+#define MPS_ERR_NONFINITE 5    /* NaN/Inf met in a singular value           */
+
+/* Per-job status bits written by mps_apply_2q_batch. */
+#define MPS_STATUS_NOT_CONVERGED 1
+#define MPS_STATUS_NONFINITE 2
+
+typedef struct { float re, im; } mps_c64;
+
+/* One two-qudit gate on adjacent sites (left site a, right site b).
+ * 88 bytes, naturally aligned; the Python side mirrors it field by field. */
+typedef struct {
+    const mps_c64* a;      /* (chi_l, d, chi_m)                            */
+    const mps_c64* b;      /* (chi_m, d, chi_r)                            */
+    const mps_c64* gate;   /* (d*d, d*d) row-major G[(a'b'),(ab)]          */
+    mps_c64* a_out;        /* (chi_l, d, k): new left site                 */
+    mps_c64* b_out;        /* (k, d, chi_r): new right site                */
+    float* svals;          /* optional: min(m,n) singular values, descending */
+    double* discarded;     /* optional: sum of squares of dropped values   */
+    int32_t* status;       /* optional: MPS_STATUS_* bits for this job     */
+    int32_t chi_l, chi_m, chi_r;
+    int32_t k;             /* kept count, 0 <= k <= min(chi_l*d, d*chi_r)  */
+    int32_t keep_left_canonical; /* 1: left=U, right=S.V^H; 0: U.S, V^H   */
+    int32_t pad0;
+} mps_2q_job;
+
+/* Solver controls for the Jacobi SVD (zero fields take the defaults). */
+typedef struct {
+    int32_t max_sweeps;    /* default 40                                   */
+    float tol;             /* relative off-diagonal threshold; default
+                              sqrt(rows) * 2^-24, at least 2^-23           */
+    int32_t block_cols;    /* columns per block: 8 or 16 (default 16)      */
+    int32_t sweeps_out;    /* out: sweeps taken by the slowest job         */
+} mps_svd_params;
+
+/* Library version and build description. */
+int mps_version(void);
+const char* mps_last_error(void);
+/* Kernel launches this library has issued in the process so far. */
+unsigned long long mps_kernel_launches(void);
+
+/* One-qudit gate in place: site[l,a',r] = sum_a U[a',a] site[l,a,r].
+ * Replaces MPS.apply_one_qudit_gate, unitary branch (mpsim/core.py:753-826). */
+int mps_apply_1q(void* stream, mps_c64* site, int chi_l, int d, int chi_r,
+                 const mps_c64* gate);
+
+/* Workspace bytes mps_apply_2q_batch needs for njobs jobs whose merged
+ * matrices are at most max_m x max_n (m = chi_l*d, n = d*chi_r). */
+size_t mps_2q_workspace_bytes(int njobs, int max_m, int max_n, int d);
+
+/* Applies njobs independent two-qudit gates (jobs_dev: a device array of
+ * mps_2q_job; the sites of different jobs must not alias).  Per job: merge
+ * A.B with the gate fused in (theta = (chi_l*d) x (d*chi_r)), block one-sided
+ * Jacobi SVD, descending sort, truncation to k values, and the regauge with
+ * the singular values placed as keep_left_canonical asks.  max_m/max_n bound
+ * every job's theta; the host must know them.  Blocks the calling thread
+ * once per Jacobi sweep to test convergence.
+ * Replaces MPS.apply_two_qudit_gate for adjacent sites (mpsim/core.py:
+ * 1059-1152: merge 1059-1062, gate 1064-1068, truncated SVD 1132-1137 via
+ * TensorNetwork split_node_full_svd, S placement 1139-1145). */
+int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs_dev, int njobs,
+                       int max_m, int max_n, int d, void* workspace,
+                       size_t workspace_bytes, mps_svd_params* params);
+
+/* Workspace bytes for the contractions below (sites of at most max_chi). */
+size_t mps_sweep_workspace_bytes(int max_chi, int d);
+
+/* <a|b>-style overlap, reference convention: sum_x a(x) * conj(b(x)).
+ * a_sites/b_sites: host arrays of n device pointers; chis: host array of
+ * n+1 bond dimensions for a (chi_0 = chi_n = 1), chis_b likewise for b.
+ * Writes the complex result to *result_host (blocks until done).
+ * Replaces MPS.inner_product / MPS.norm (mpsim/core.py:507-565). */
+int mps_inner_product(void* stream, const mps_c64* const* a_sites,
+                      const int* chis_a, const mps_c64* const* b_sites,
+                      const int* chis_b, int n, int d, void* workspace,
+                      size_t workspace_bytes, double* result_host);
+
+/* Full state vector psi[x_0 ... x_{n-1}] (qudit 0 most significant) into
+ * out_dev (d**n elements).  workspace: 2 * d**n complex64 plus slack.
+ * Replaces MPS.wavefunction (mpsim/core.py:483-500). */
+int mps_wavefunction(void* stream, const mps_c64* const* sites,
+                     const int* chis, int n, int d, mps_c64* out_dev,
+                     void* workspace, size_t workspace_bytes);
+
+/* Amplitudes <x|psi> for nbits bitstrings (bits_dev: nbits x n int8,
+ * row-major) into out_dev (nbits complex64).  workspace:
+ * 2 * nbits * d * max_chi complex64. */
+int mps_amplitudes(void* stream, const mps_c64* const* sites, const int* chis,
+                   int n, int d, const int8_t* bits_dev, int nbits,
+                   mps_c64* out_dev, void* workspace, size_t workspace_bytes);
+
+/* site[i] = alpha * (conj ? conj(site[i]) : site[i]) for count elements.
+ * Used by MPS.renormalize (mpsim/core.py:567-594, scale every site by
+ * (to/norm)^(1/n)) and MPS.dagger (core.py:502-505, conj every site). */
+int mps_scale(void* stream, mps_c64* site, size_t count, float alpha_re,
+              float alpha_im, int conj);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPSIM_GB300_H */

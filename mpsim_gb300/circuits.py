@@ -1,0 +1,127 @@
+"""Seeded synthetic brickwork circuits (the benchmark and parity workloads).
+
+Every gate is drawn by ``haar_random_matrix`` (mpsim/gates.py:248-286) with an
+explicit 32-bit seed derived from (base seed, instance, layer, slot, kind), so
+any single gate of any circuit can be regenerated on its own.  Layer t applies
+a one-qudit Haar U(d) to every site, then two-qudit Haar U(d^2) gates on the
+pairs (2j, 2j+1) for even t and (2j+1, 2j+2) for odd t.
+
+Workloads (qubit count, depth, truncation) named by their sizes:
+  brickwork_10q_d10_full     10 qubits, depth 10, no truncation
+  brickwork_48q_d24_chi128   48 qubits, depth 24, maxsvals=128
+  brickwork_64q_d40_chi256   64 qubits, depth 40, maxsvals=256 (theta 512x512)
+  batch_512_mixed            512 circuits, 16-48 qubits, depth 8-32,
+                             maxsvals in {16,32,64,128}, 20% CNOT/CZ slots
+  qutrit_128x32_d30_chi192   128 circuits of 32 qutrits, depth 30, maxsvals=192
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from .gates import haar_random_matrix, _cnot_matrix
+
+KIND_1Q = 1
+KIND_2Q = 2
+
+
+def gate_seed(base: int, instance: int, layer: int, slot: int, kind: int) -> int:
+    """32-bit RandomState seed for one gate."""
+    ss = np.random.SeedSequence([base, instance, layer, slot, kind])
+    return int(ss.generate_state(1, dtype=np.uint32)[0])
+
+
+@dataclass
+class Layer:
+    one_q: np.ndarray              # (n, d, d) complex128: U[a', a] per site
+    pair_left: np.ndarray          # (p,) int: left site of each pair
+    two_q: np.ndarray              # (p, d*d, d*d) complex128: U[(a'b'),(ab)]
+
+
+@dataclass
+class BrickworkCircuit:
+    nqudits: int
+    d: int
+    depth: int
+    maxsvals: Optional[int]
+    seed: int = 0
+    instance: int = 0
+    layers: List[Layer] = field(default_factory=list)
+
+    @property
+    def n_two_qudit_gates(self) -> int:
+        return int(sum(len(l.pair_left) for l in self.layers))
+
+    @property
+    def n_one_qudit_gates(self) -> int:
+        return int(sum(l.one_q.shape[0] for l in self.layers))
+
+    def operations(self):
+        """Gates in application order as (kind, sites, matrix)."""
+        for lay in self.layers:
+            for i in range(self.nqudits):
+                yield (1, (i,), lay.one_q[i])
+            for p, i in enumerate(lay.pair_left):
+                yield (2, (int(i), int(i) + 1), lay.two_q[p])
+
+
+def brickwork(nqudits: int, depth: int, d: int = 2, maxsvals: Optional[int] = None,
+              seed: int = 0, instance: int = 0, special_fraction: float = 0.0
+              ) -> BrickworkCircuit:
+    """Seeded brickwork circuit; ``special_fraction`` of the two-qudit slots
+    (qubits only) hold a fixed CNOT or CZ instead of a Haar unitary."""
+    circ = BrickworkCircuit(nqudits, d, depth, maxsvals, seed, instance)
+    pick = np.random.default_rng(np.random.SeedSequence([seed, instance, 7919]))
+    cz = np.diag([1, 1, 1, -1]).astype(np.complex128)
+    cn = _cnot_matrix.reshape(4, 4).astype(np.complex128)
+    for t in range(depth):
+        one = np.stack([haar_random_matrix(1, d, gate_seed(seed, instance, t, i, KIND_1Q))
+                        for i in range(nqudits)])
+        start = t % 2
+        lefts = np.arange(start, nqudits - 1, 2, dtype=np.int64)
+        twos = []
+        for i in lefts:
+            if special_fraction > 0 and pick.random() < special_fraction:
+                twos.append(cn if pick.random() < 0.5 else cz)
+            else:
+                twos.append(haar_random_matrix(2, d, gate_seed(seed, instance, t, int(i), KIND_2Q)))
+        two = np.stack(twos) if twos else np.zeros((0, d * d, d * d), np.complex128)
+        circ.layers.append(Layer(one, lefts, two))
+    return circ
+
+
+WORKLOADS = {
+    "brickwork_10q_d10_full": dict(nqudits=10, depth=10, d=2, maxsvals=None),
+    "brickwork_48q_d24_chi128": dict(nqudits=48, depth=24, d=2, maxsvals=128),
+    "brickwork_64q_d40_chi256": dict(nqudits=64, depth=40, d=2, maxsvals=256),
+}
+
+
+def workload(name: str, seed: int = 0, instance: int = 0) -> BrickworkCircuit:
+    return brickwork(seed=seed, instance=instance, **WORKLOADS[name])
+
+
+def mixed_batch(ncircuits: int = 512, seed: int = 0) -> List[BrickworkCircuit]:
+    """512 independent circuits: qubits U[16,48], depth U[8,32],
+    maxsvals from {16,32,64,128}, 20% of two-qubit slots CNOT or CZ."""
+    out = []
+    for k in range(ncircuits):
+        rng = np.random.default_rng(np.random.SeedSequence([seed, k, 104729]))
+        nq = int(rng.integers(16, 49))
+        depth = int(rng.integers(8, 33))
+        chi = int(rng.choice([16, 32, 64, 128]))
+        out.append(brickwork(nq, depth, 2, chi, seed, k, special_fraction=0.2))
+    return out
+
+
+def qutrit_batch(ncircuits: int = 128, seed: int = 0) -> List[BrickworkCircuit]:
+    """128 circuits of 32 qutrits, depth 30, maxsvals=192 (theta <= 576x576)."""
+    return [brickwork(32, 30, 3, 192, seed, k) for k in range(ncircuits)]
+
+
+def sample_bitstrings(nqudits: int, d: int, count: int = 4096, seed: int = 0) -> np.ndarray:
+    """Seeded computational-basis bitstrings for amplitude checks."""
+    return np.random.default_rng(seed).integers(0, d, (count, nqudits))

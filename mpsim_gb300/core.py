@@ -1,0 +1,839 @@
+"""MPS state and operations with mpsim's API (mpsim/core.py), on one GPU.
+
+Site tensors live on the GPU as torch complex64 tensors of shape
+(chi_left, d, chi_right).  Every state-changing or state-reading operation
+runs in the sm_103a kernels of ``libmpsim_gb300.so`` (see
+include/mpsim_gb300.h); Python only validates arguments (with mpsim's
+exception types and conditions), plans shapes and owns memory.  There is no
+CPU fallback: without the library or a CUDA device the constructor raises.
+
+Differences from the reference, all deliberate:
+* complex64 storage throughout (the reference silently promotes to
+  complex128 when it meets the float64 ``cnot``/``swap`` or complex128 Haar
+  gates; here every gate is cast to complex64 first);
+* the per-gate norm history ``_norms`` (mpsim/core.py:1160-1161, marked
+  "TODO: Remove ... only for convenience in benchmarking") is opt-in via
+  ``track_norms=True``: it is a full O(n d chi^3) sweep after every gate;
+* ``apply`` runs consecutive two-qudit gates on disjoint adjacent pairs as
+  one batched launch -- exact, because each merged matrix depends only on its
+  own two sites;
+* ``get_node(s)`` return host copies (TensorNetwork-like nodes with the
+  reference's initial axis order: physical axis first);
+* non-unitary one-qudit gates with orthonormalisation, sampling, reduced
+  density matrices and ``from_wavefunction`` are outside this build's hot
+  path and raise NotImplementedError.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import warnings
+from copy import deepcopy
+from typing import List, Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from . import _native
+from .gates import (Node, cnot, gate_tensor, haar_random_unitary, hgate, is_hermitian,
+                    is_unitary, rgate, swap, xgate)
+
+try:
+    import torch
+except ImportError:  # pragma: no cover - torch is a hard dependency on GPU hosts
+    torch = None
+
+
+class CannotConvertToMPSOperation(Exception):
+    pass
+
+
+# ---------------------------------------------------------------------------
+# Host-side helpers (pure Python; unit-tested on CPU)
+
+def _edges_of(gate):
+    """(number of dangling edges, number of connected edges, dims)."""
+    t = gate_tensor(gate)
+    dims = tuple(int(x) for x in t.shape)
+    if hasattr(gate, "get_all_dangling") and hasattr(gate, "get_all_nondangling"):
+        return len(gate.get_all_dangling()), len(gate.get_all_nondangling()), dims
+    return len(dims), 0, dims
+
+
+def kept_count(maxsvals: Optional[int], rank: int) -> int:
+    """Singular values kept for ``max_singular_values=maxsvals``.
+
+    TensorNetwork keeps ``s[:min(maxsvals, rank)]``; a negative value acts like
+    a Python slice stop, which this reproduces.
+    """
+    if maxsvals is None:
+        return rank
+    return len(range(rank)[:min(int(maxsvals), rank)])
+
+
+def parse_truncation(kwargs: dict, max_bond_dimension_of, index: int) -> Optional[int]:
+    """``fraction`` / ``maxsvals`` handling of mpsim/core.py:1110-1130.
+
+    ``index`` is min(node_index1, node_index2) after the swap network.
+    Returns the ``max_singular_values`` argument (None keeps everything).
+    """
+    if "fraction" in kwargs and "maxsvals" in kwargs:
+        raise ValueError("Only one of (fraction, maxsvals) can be provided as kwargs.")
+    maxsvals = None
+    if "fraction" in kwargs:
+        fraction = kwargs.get("fraction")
+        if not (0 <= fraction <= 1):
+            raise ValueError("Keyword fraction must be between 0 and 1 but is", fraction)
+        maxsvals = int(round(fraction * max_bond_dimension_of(index)))
+    if "maxsvals" in kwargs:
+        maxsvals = int(kwargs.get("maxsvals"))
+    return maxsvals
+
+
+def max_bond_dimensions(nqudits: int, d: int) -> List[int]:
+    """mpsim/core.py:235-242."""
+    half = [d ** (i + 1) for i in range(nqudits // 2)]
+    out = half + list(reversed(half))
+    if nqudits % 2 == 0:
+        out.remove(d ** (nqudits // 2))
+    return out
+
+
+def _require_cuda():
+    if torch is None or not torch.cuda.is_available():
+        raise RuntimeError(
+            "mpsim_gb300 runs on a CUDA GPU only (no CPU fallback); no CUDA device is visible")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+class _Workspace:
+    """Grow-only device scratch buffers, one pool per device."""
+
+    def __init__(self):
+        self._buf = {}
+
+    def get(self, device, nbytes: int, slot: str = "main"):
+        key = (str(device), slot)
+        cur = self._buf.get(key)
+        if cur is None or cur.numel() < nbytes:
+            size = max(int(nbytes), 1 << 20)
+            if cur is not None:
+                size = max(size, int(cur.numel() * 1.25))
+            cur = torch.empty(size, dtype=torch.uint8, device=device)
+            self._buf[key] = cur
+        return cur
+
+
+_WS = _Workspace()
+
+
+def _ptr_array(tensors):
+    arr = (ctypes.c_void_p * len(tensors))()
+    for i, t in enumerate(tensors):
+        arr[i] = t.data_ptr() if t.numel() > 0 else 0
+    return arr
+
+
+def _int_array(vals):
+    arr = (ctypes.c_int * len(vals))()
+    for i, v in enumerate(vals):
+        arr[i] = int(v)
+    return arr
+
+
+# ---------------------------------------------------------------------------
+
+class MPSOperation:
+    """An operation on one or two qudits (mpsim/core.py:21-156)."""
+
+    def __init__(self, node, qudit_indices: Union[int, Tuple[int, ...]],
+                 qudit_dimension: int = 2) -> None:
+        self._node = node
+        if isinstance(qudit_indices, (int, np.integer)):
+            qudit_indices = (int(qudit_indices),)
+        self._qudit_indices = tuple(qudit_indices)
+        self._qudit_dimension = int(qudit_dimension)
+
+    @property
+    def qudit_indices(self) -> Tuple[int, ...]:
+        return self._qudit_indices
+
+    @property
+    def qudit_dimension(self) -> int:
+        return self._qudit_dimension
+
+    @property
+    def num_qudits(self) -> int:
+        return len(self._qudit_indices)
+
+    def node(self, copy: bool = True):
+        if not copy:
+            return self._node
+        return Node(deepcopy(gate_tensor(self._node)), name=getattr(self._node, "name", None))
+
+    def tensor(self, reshape_to_square_matrix: bool = True) -> np.ndarray:
+        t = deepcopy(gate_tensor(self._node))
+        if reshape_to_square_matrix:
+            dim = self._qudit_dimension ** self.num_qudits
+            t = np.reshape(t, (dim, dim))
+        return t
+
+    def is_valid(self) -> bool:
+        d = self._qudit_dimension
+        ndang, nconn, dims = _edges_of(self._node)
+        if dims != tuple([d] * 2 * self.num_qudits):
+            return False
+        if ndang + nconn != 2 * self.num_qudits:
+            return False
+        if nconn:
+            return False
+        return True
+
+    def is_unitary(self) -> bool:
+        return is_unitary(self.tensor(reshape_to_square_matrix=True))
+
+    def is_hermitian(self) -> bool:
+        return is_hermitian(self.tensor(reshape_to_square_matrix=True))
+
+    def is_single_qudit_operation(self) -> bool:
+        return self.num_qudits == 1
+
+    def is_two_qudit_operation(self) -> bool:
+        return self.num_qudits == 2
+
+    def __str__(self):
+        return f"Tensor {getattr(self._node, 'name', '')} on qudit(s) {self._qudit_indices}."
+
+
+class MPS:
+    """Matrix product state on one GPU (mpsim/core.py:159-1423)."""
+
+    def __init__(self, nqudits: int, qudit_dimension: int = 2, tensor_prefix: str = "q",
+                 *, track_norms: bool = False, record_svals: bool = False) -> None:
+        if nqudits < 2:
+            raise ValueError(f"Number of qudits must be greater than 2 but is {nqudits}.")
+        self._nqudits = int(nqudits)
+        self._qudit_dimension = int(qudit_dimension)
+        self._prefix = tensor_prefix
+        self._max_bond_dimensions = max_bond_dimensions(self._nqudits, self._qudit_dimension)
+        self._norms = []  # type: List[float]
+        self.track_norms = track_norms
+        self.record_svals = record_svals
+        self.svals_history = []
+        self.svd_params = _native.SvdParams()
+        # When a list, each batched two-qudit launch appends
+        # (jobs, max_m, max_n, sweeps, start_event, end_event).
+        self.timing = None
+        self._device = _require_cuda()
+        d = self._qudit_dimension
+        init = torch.zeros((self._nqudits, 1, d, 1), dtype=torch.complex64)
+        init[:, 0, 0, 0] = 1.0
+        init = init.to(self._device)
+        self._sites = [init[i].clone() for i in range(self._nqudits)]
+
+    # -- plumbing ----------------------------------------------------------
+    @property
+    def device(self):
+        return self._device
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self._device).cuda_stream)
+
+    def _lib(self):
+        return _native.load()
+
+    def _to_device_gate(self, mat: np.ndarray):
+        g = np.ascontiguousarray(np.asarray(mat).astype(np.complex64))
+        return torch.from_numpy(g).to(self._device)
+
+    @property
+    def sites(self):
+        """The device site tensors, (chi_left, d, chi_right) complex64."""
+        return list(self._sites)
+
+    # -- structure ---------------------------------------------------------
+    @property
+    def nqudits(self) -> int:
+        return self._nqudits
+
+    @property
+    def qudit_dimension(self) -> int:
+        return self._qudit_dimension
+
+    def bond_dimension_of(self, node_index: int) -> int:
+        if not self.is_valid():
+            raise ValueError("MPS is invalid.")
+        if node_index >= self._nqudits:
+            raise ValueError(f"Index should be less than {self._nqudits} but is {node_index}.")
+        if node_index == self._nqudits - 1:
+            raise IndexError("list index out of range")
+        if node_index < 0:
+            if self._nqudits == 2 and node_index == -1:
+                raise ValueError("Non-connected graph")
+            raise ValueError("Non-connected graph")
+        return int(self._sites[node_index].shape[2])
+
+    def bond_dimensions(self) -> List[int]:
+        return [self.bond_dimension_of(i) for i in range(self._nqudits - 1)]
+
+    def max_bond_dimension_of(self, edge_index: int) -> int:
+        if edge_index >= self._nqudits:
+            raise ValueError(f"Edge index should be less than {self._nqudits} but is {edge_index}.")
+        return self._max_bond_dimensions[edge_index]
+
+    def max_bond_dimensions(self) -> List[int]:
+        return self._max_bond_dimensions
+
+    def is_valid(self) -> bool:
+        s = self._sites
+        if len(s) < 2:
+            return False
+        d = self._qudit_dimension
+        if s[0].shape[0] != 1 or s[-1].shape[2] != 1:
+            return False
+        for i, t in enumerate(s):
+            if t.dim() != 3 or t.shape[1] != d:
+                return False
+            if i < len(s) - 1 and t.shape[2] != s[i + 1].shape[0]:
+                print(f"Nodes at index {i} and {i + 1} are not connected.")
+                return False
+        return True
+
+    def _chis(self, sites=None):
+        sites = self._sites if sites is None else sites
+        return [int(sites[0].shape[0])] + [int(t.shape[2]) for t in sites]
+
+    def get_nodes(self, copy: bool = True) -> List[Node]:
+        """Host copies of the site tensors, physical axis first:
+        (d, chi) for the end sites, (d, chi_left, chi_right) inside."""
+        out = []
+        n = self._nqudits
+        for i, t in enumerate(self._sites):
+            a = t.detach().cpu().numpy()
+            a = np.transpose(a, (1, 0, 2))
+            if i == 0:
+                a = a[:, 0, :]
+            elif i == n - 1:
+                a = a[:, :, 0]
+            out.append(Node(a.copy(), name=self._prefix + str(i)))
+        return out
+
+    def get_node(self, node_index: int, copy: bool = True) -> Node:
+        return self.get_nodes(copy)[node_index]
+
+    # -- contractions ------------------------------------------------------
+    def wavefunction(self) -> np.ndarray:
+        """Full state vector, qudit 0 most significant (core.py:483-500)."""
+        if not self.is_valid():
+            raise ValueError("MPS is not valid.")
+        d, n = self._qudit_dimension, self._nqudits
+        size = d ** n
+        if size > (1 << 31):
+            raise ValueError(f"wavefunction of {size} amplitudes is too large")
+        chis = self._chis()
+        need, p = 1, 1
+        for i in range(n):
+            p *= d
+            need = max(need, p * max(chis[i + 1], 1))
+        ws = _WS.get(self._device, 2 * need * 8, "wf")
+        out = torch.empty(size, dtype=torch.complex64, device=self._device)
+        _native.check(self._lib().mps_wavefunction(
+            self._stream(), _ptr_array(self._sites), _int_array(chis), n, d,
+            ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ws.data_ptr()), ws.numel()))
+        return out.cpu().numpy()
+
+    def amplitudes(self, bitstrings) -> np.ndarray:
+        """<x|psi> for each row of ``bitstrings`` (shape (S, nqudits))."""
+        bits = np.ascontiguousarray(np.asarray(bitstrings, dtype=np.int8))
+        if bits.ndim != 2 or bits.shape[1] != self._nqudits:
+            raise ValueError("bitstrings must have shape (count, nqudits)")
+        if bits.size and (bits.min() < 0 or bits.max() >= self._qudit_dimension):
+            raise ValueError("bitstring digits must lie in [0, qudit_dimension)")
+        nb = bits.shape[0]
+        if nb == 0:
+            return np.zeros(0, np.complex64)
+        chis = self._chis()
+        mx = max(chis)
+        d = self._qudit_dimension
+        ws = _WS.get(self._device, (nb * d * mx + 2 * nb * mx) * 8, "amp")
+        bdev = torch.from_numpy(bits).to(self._device)
+        out = torch.empty(nb, dtype=torch.complex64, device=self._device)
+        _native.check(self._lib().mps_amplitudes(
+            self._stream(), _ptr_array(self._sites), _int_array(chis), self._nqudits, d,
+            ctypes.c_void_p(bdev.data_ptr()), nb, ctypes.c_void_p(out.data_ptr()),
+            ctypes.c_void_p(ws.data_ptr()), ws.numel()))
+        return out.cpu().numpy()
+
+    def dagger(self) -> None:
+        """Conjugates every site (core.py:502-505)."""
+        for t in self._sites:
+            _native.check(self._lib().mps_scale(self._stream(), ctypes.c_void_p(t.data_ptr()),
+                                                t.numel(), 1.0, 0.0, 1))
+
+    def inner_product(self, other: "MPS") -> complex:
+        """sum_x self(x) * conj(other(x)) (core.py:507-561)."""
+        if other._nqudits != self._nqudits:
+            raise ValueError(
+                f"Cannot compute inner product between self which has {self._nqudits} qudits "
+                f"and other which has {other._nqudits} qudits.\nNumber of qudits must be equal.")
+        if other._qudit_dimension != self._qudit_dimension:
+            raise ValueError(
+                f"Cannot compute inner product between self which has qudit dimension "
+                f"{self._qudit_dimension} and other which as qudit dimension "
+                f"{other._qudit_dimension}.Qudit dimensions must be equal.")
+        if not self.is_valid():
+            raise ValueError("MPS is invalid.")
+        if not other.is_valid():
+            raise ValueError("Other MPS is invalid.")
+        ca, cb = self._chis(), other._chis()
+        mx = max(max(ca), max(cb))
+        nbytes = self._lib().mps_sweep_workspace_bytes(mx, self._qudit_dimension)
+        ws = _WS.get(self._device, nbytes, "sweep")
+        res = (ctypes.c_double * 2)()
+        _native.check(self._lib().mps_inner_product(
+            self._stream(), _ptr_array(self._sites), _int_array(ca), _ptr_array(other._sites),
+            _int_array(cb), self._nqudits, self._qudit_dimension, ctypes.c_void_p(ws.data_ptr()),
+            ws.numel(), res))
+        return complex(res[0], res[1])
+
+    def norm(self) -> float:
+        """sqrt(Re <self|self>) (core.py:563-565)."""
+        return np.sqrt(self.inner_product(self).real)
+
+    def renormalize(self, to_norm: float = 1.0) -> None:
+        """Scales every site by (to_norm / norm)^(1/n) (core.py:567-594)."""
+        if to_norm < 0.0:
+            raise ValueError(f"Arg to_norm must be positive but is {to_norm}")
+        if np.isclose(to_norm, 0.0, atol=1e-15):
+            raise ValueError(f"Arg to_norm = {to_norm} is too close to numerical zero.")
+        norm = self.norm()
+        if np.isclose(norm, 0.0, atol=1e-15):
+            raise ValueError("Norm of MPS is numerically zero, cannot renormalize.")
+        factor = float((to_norm / norm) ** (1 / self._nqudits))
+        for t in self._sites:
+            _native.check(self._lib().mps_scale(self._stream(), ctypes.c_void_p(t.data_ptr()),
+                                                t.numel(), factor, 0.0, 0))
+
+    def expectation(self, observable: MPSOperation) -> float:
+        """<mps|O|mps> (core.py:723-751)."""
+        if not observable.is_hermitian():
+            raise ValueError("Observable is not Hermitian.")
+        if observable.qudit_dimension != self._qudit_dimension:
+            od, md = observable.qudit_dimension, self._qudit_dimension
+            raise ValueError(
+                f"Dimension mismatch between observable and MPS. Observable is ({od}, {od}) "
+                f"but MPS has qudit dimension {md}.")
+        other = self.copy()
+        other.apply(observable)
+        return self.inner_product(other).real
+
+    def reduced_density_matrix(self, node_indices):
+        raise NotImplementedError("reduced_density_matrix is outside this build's scope")
+
+    def sample(self, nsamples: int, as_hist: bool = False, as_string: bool = False):
+        raise NotImplementedError("sampling is outside this build's scope")
+
+    @staticmethod
+    def from_wavefunction(wavefunction, nqudits, qudit_dimension=2, tensor_prefix="q"):
+        raise NotImplementedError("from_wavefunction is outside this build's scope")
+
+    def orthonormalize_right_edge_of(self, node_index: int, threshold: float = 1e-8):
+        raise NotImplementedError("orthonormalization is outside this build's scope")
+
+    def orthonormalize_left_edge_of(self, node_index: int, threshold: float = 1e-8):
+        raise NotImplementedError("orthonormalization is outside this build's scope")
+
+    # -- one-qudit gates ---------------------------------------------------
+    def _check_one_qudit(self, gate, node_index):
+        if not self.is_valid():
+            raise ValueError("MPS is invalid.")
+        if node_index not in range(self._nqudits):
+            raise ValueError(f"Input tensor index={node_index} is out of bounds for"
+                             f" an MPS on {self._nqudits} qudits.")
+        ndang, nconn, dims = _edges_of(gate)
+        if ndang != 2 or nconn != 0:
+            raise ValueError("Single qudit gate must have two free edges and zero connected edges.")
+        if dims[0] != dims[1]:
+            raise ValueError("Gate edge dimensions must be equal.")
+        if dims[0] != self._qudit_dimension:
+            raise ValueError(f"Gate edges have dimension {dims[0]} but should have MPS qudit "
+                             f"dimension = {self._qudit_dimension}")
+
+    def apply_one_qudit_gate(self, gate, node_index: int, **kwargs) -> None:
+        """site[l,a',r] = sum_a U[a',a] site[l,a,r] (core.py:753-845)."""
+        self._check_one_qudit(gate, node_index)
+        mat = gate_tensor(gate)
+        unitary = is_unitary(np.asarray(mat))
+        renorm = kwargs.get("renormalize_after_non_unitary") is not False
+        ortho = kwargs.get("ortho_after_non_unitary") is not False
+        if not unitary and ortho:
+            raise NotImplementedError(
+                "non-unitary one-qudit gates with ortho_after_non_unitary=True are outside "
+                "this build's scope; pass ortho_after_non_unitary=False")
+        norm = self.norm() if (not unitary and renorm) else None
+        site = self._sites[node_index]
+        g = self._to_device_gate(mat)
+        _native.check(self._lib().mps_apply_1q(
+            self._stream(), ctypes.c_void_p(site.data_ptr()), int(site.shape[0]),
+            self._qudit_dimension, int(site.shape[2]), ctypes.c_void_p(g.data_ptr())))
+        if norm is not None:
+            self.renormalize(norm)
+
+    def apply_one_qudit_gate_to_all(self, gate) -> None:
+        for i in range(self._nqudits):
+            self.apply_one_qudit_gate(gate, i)
+
+    # -- two-qudit gates ---------------------------------------------------
+    def _check_two_qudit(self, gate, i, j):
+        if not self.is_valid():
+            raise ValueError("MPS is not valid.")
+        if i not in range(self._nqudits) or j not in range(self._nqudits):
+            raise ValueError(f"Input tensor indices={(i, j)} are out of "
+                             f"bounds for an MPS on {self._nqudits} qudits.")
+        if i == j:
+            raise ValueError("Node indices cannot be identical.")
+        ndang, nconn, dims = _edges_of(gate)
+        if ndang != 4 or nconn != 0:
+            raise ValueError("Two qubit gate must have four free edges and zero connected edges.")
+        if len(set(dims)) != 1:
+            raise ValueError("All gate edges must have the same dimension.")
+        if dims[0] != self._qudit_dimension:
+            raise ValueError(f"Gate edges have dimension {dims[0]} but should have MPS qudit "
+                             f"dimension = {self._qudit_dimension}")
+
+    def _prepare_pair(self, gate, i, j, kwargs):
+        """Validate, flip, and return (G (d^2 x d^2) complex64, left, k, lc)
+        for an ADJACENT pair.  Mirrors core.py:1000-1033 and 1104-1130."""
+        self._check_two_qudit(gate, i, j)
+        d = self._qudit_dimension
+        g = np.asarray(gate_tensor(gate)).reshape((d,) * 4)
+        if j < i:
+            g = g.transpose(1, 0, 3, 2)
+            i, j = j, i
+        lc = kwargs["keep_left_canonical"] if "keep_left_canonical" in kwargs else True
+        maxsvals = parse_truncation(kwargs, self.max_bond_dimension_of, min(i, j))
+        a, b = self._sites[i], self._sites[j]
+        m = int(a.shape[0]) * d
+        n = int(b.shape[2]) * d
+        k = kept_count(maxsvals, min(m, n))
+        return g.reshape(d * d, d * d).astype(np.complex64), i, k, bool(lc)
+
+    def apply_two_qudit_gate(self, gate, node_index1: int, node_index2: int, **kwargs) -> None:
+        """Two-qudit gate with truncated SVD (core.py:950-1161)."""
+        self._check_two_qudit(gate, node_index1, node_index2)
+        d = self._qudit_dimension
+        g = np.asarray(gate_tensor(gate)).reshape((d,) * 4)
+        i, j = node_index1, node_index2
+        if j < i:
+            g = g.transpose(1, 0, 3, 2)
+            i, j = j, i
+        invert = False
+        if i < j - 1:
+            invert = True
+            original = i
+            self.move_node_from_left_to_right(i, j - 1, **kwargs)
+            i = j - 1
+        mat, left, k, lc = self._prepare_pair(g, i, j, kwargs)
+        self._run_pairs([(mat, left, k, lc)])
+        if invert:
+            self.move_node_from_right_to_left(i, original, **kwargs)
+        if self.track_norms:
+            self._norms.append(self.norm())
+
+    def _run_pairs(self, pairs):
+        """One batched launch for two-qudit gates on disjoint adjacent pairs."""
+        if not pairs:
+            return
+        d = self._qudit_dimension
+        dev = self._device
+        njobs = len(pairs)
+        if all(isinstance(p[0], torch.Tensor) for p in pairs):
+            gates = torch.stack([p[0].reshape(d * d, d * d) for p in pairs]).to(
+                dev, torch.complex64).contiguous()
+        else:
+            gates = torch.from_numpy(np.ascontiguousarray(
+                np.stack([np.asarray(p[0]) for p in pairs]).astype(np.complex64))).to(dev)
+        table = np.zeros(njobs, dtype=_native.JOB_DTYPE)
+        outs = []
+        max_m = max_n = 1
+        rec = self.record_svals
+        svals = disc = None
+        status = torch.zeros(njobs, dtype=torch.int32, device=dev)
+        if rec:
+            rmax = max(min(int(self._sites[p[1]].shape[0]) * d, int(self._sites[p[1] + 1].shape[2]) * d)
+                       for p in pairs)
+            svals = torch.zeros((njobs, max(rmax, 1)), dtype=torch.float32, device=dev)
+            disc = torch.zeros(njobs, dtype=torch.float64, device=dev)
+        for q, (mat, left, k, lc) in enumerate(pairs):
+            a, b = self._sites[left], self._sites[left + 1]
+            chil, chim, chir = int(a.shape[0]), int(a.shape[2]), int(b.shape[2])
+            a_out = torch.empty((chil, d, k), dtype=torch.complex64, device=dev)
+            b_out = torch.empty((k, d, chir), dtype=torch.complex64, device=dev)
+            outs.append((left, a_out, b_out))
+            max_m = max(max_m, chil * d)
+            max_n = max(max_n, chir * d)
+            row = table[q]
+            row["a"] = a.data_ptr()
+            row["b"] = b.data_ptr()
+            row["gate"] = gates[q].data_ptr()
+            row["a_out"] = a_out.data_ptr() if a_out.numel() else 0
+            row["b_out"] = b_out.data_ptr() if b_out.numel() else 0
+            row["svals"] = svals[q].data_ptr() if rec else 0
+            row["discarded"] = disc[q].data_ptr() if rec else 0
+            row["status"] = status[q].data_ptr()
+            row["chi_l"], row["chi_m"], row["chi_r"] = chil, chim, chir
+            row["k"] = k
+            row["keep_left_canonical"] = 1 if lc else 0
+        jobs = torch.from_numpy(table.view(np.uint8)).to(dev)
+        lib = self._lib()
+        nbytes = lib.mps_2q_workspace_bytes(njobs, max_m, max_n, d)
+        ws = _WS.get(dev, nbytes, "2q")
+        timing = self.timing
+        if timing is not None:
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(torch.cuda.current_stream(dev))
+        rc = lib.mps_apply_2q_batch(self._stream(), ctypes.c_void_p(jobs.data_ptr()), njobs,
+                                    max_m, max_n, d, ctypes.c_void_p(ws.data_ptr()), ws.numel(),
+                                    ctypes.byref(self.svd_params))
+        if timing is not None:
+            ev1.record(torch.cuda.current_stream(dev))
+            timing.append((njobs, max_m, max_n, self.svd_params.sweeps_out, ev0, ev1))
+        if rc == _native.MPS_ERR_NOT_CONVERGED:
+            warnings.warn("mpsim_gb300: " + _native.last_error(), RuntimeWarning)
+        elif rc != _native.MPS_OK:
+            raise _native.NativeError(rc, _native.last_error())
+        for left, a_out, b_out in outs:
+            self._sites[left] = a_out
+            self._sites[left + 1] = b_out
+        if rec:
+            sv = svals.cpu().numpy()
+            dc = disc.cpu().numpy()
+            for q, (mat, left, k, lc) in enumerate(pairs):
+                a_out = outs[q][1]
+                r = min(int(a_out.shape[0]) * d, int(outs[q][2].shape[2]) * d)
+                self.svals_history.append((sv[q, :r].astype(np.float64), k, float(dc[q])))
+
+    def move_node_from_left_to_right(self, current_node_index: int, final_node_index: int,
+                                     **kwargs) -> None:
+        """Chain of SWAPs (core.py:1163-1190)."""
+        if current_node_index > final_node_index:
+            raise ValueError("current_node_index should be smaller than final_node_index.")
+        if current_node_index < 0:
+            raise ValueError("current_node_index out of range.")
+        if final_node_index >= self._nqudits:
+            raise ValueError("final_node_index out of range.")
+        while current_node_index < final_node_index:
+            self.swap(current_node_index, current_node_index + 1, **kwargs)
+            current_node_index += 1
+
+    def move_node_from_right_to_left(self, current_node_index: int, final_node_index: int,
+                                     **kwargs) -> None:
+        """Chain of SWAPs (core.py:1192-1219)."""
+        if current_node_index < final_node_index:
+            raise ValueError("current_node_index should be larger than final_node_index.")
+        if current_node_index > self._nqudits:
+            raise ValueError("current_node_index out of range.")
+        if final_node_index < 0:
+            raise ValueError("final_node_index out of range.")
+        while current_node_index > final_node_index:
+            self.swap(current_node_index - 1, current_node_index, **kwargs)
+            current_node_index -= 1
+
+    # -- operation lists ---------------------------------------------------
+    def apply(self, operations, **kwargs) -> None:
+        """Applies operations in order (core.py:1221-1276).
+
+        Consecutive two-qudit gates on disjoint adjacent pairs are gathered
+        into one batched launch; a one-qudit gate on a site with a pending
+        two-qudit gate (or any other operation that touches it) first
+        flushes the batch, so the result equals in-order application."""
+        try:
+            operations = iter(operations)
+        except TypeError:
+            operations = (operations,)
+        pending = []
+        busy = set()
+
+        def flush():
+            if pending:
+                self._run_pairs(pending)
+                pending.clear()
+                busy.clear()
+
+        batchable = not self.track_norms
+        for op in operations:
+            if not isinstance(op, MPSOperation):
+                flush()
+                raise TypeError("Argument operation should be of type MPSOperation but is "
+                                f"of type {type(op)}.")
+            if not op.is_valid():
+                flush()
+                raise ValueError("Input MPS Operation is not valid.")
+            if op.is_single_qudit_operation():
+                (i,) = op.qudit_indices
+                if i in busy:
+                    flush()
+                self.apply_one_qudit_gate(op.node(copy=False), i, **kwargs)
+            elif op.is_two_qudit_operation():
+                i, j = op.qudit_indices
+                adjacent = (isinstance(i, (int, np.integer)) and isinstance(j, (int, np.integer))
+                            and abs(int(i) - int(j)) == 1 and 0 <= min(i, j)
+                            and max(i, j) < self._nqudits)
+                if batchable and adjacent:
+                    if i in busy or j in busy:
+                        flush()
+                    pending.append(self._prepare_pair(op.node(copy=False), int(i), int(j), kwargs))
+                    busy.update((int(i), int(j)))
+                else:
+                    flush()
+                    self.apply_two_qudit_gate(op.node(copy=False), i, j, **kwargs)
+            else:
+                flush()
+                raise ValueError(
+                    "Only one-qudit and two-qudit gates are supported. To apply a gate on three or "
+                    "more qudits, the gate must be compiled into a sequence of one- and two-qudit "
+                    "gates.")
+        flush()
+
+    def apply_layer(self, one_qudit: Optional[np.ndarray], pair_left: Sequence[int],
+                    two_qudit: Optional[np.ndarray], **kwargs) -> None:
+        """One brickwork layer: ``one_qudit[i]`` (d x d) on every site i, then
+        ``two_qudit[p]`` (d^2 x d^2) on (pair_left[p], pair_left[p] + 1), the
+        pairs disjoint -- the same result as applying the gates one by one."""
+        if one_qudit is not None:
+            for i in range(self._nqudits):
+                self.apply_one_qudit_gate(one_qudit[i], i)
+        if two_qudit is None or len(pair_left) == 0:
+            return
+        used = set()
+        pairs = []
+        for p, i in enumerate(pair_left):
+            i = int(i)
+            if i in used or i + 1 in used:
+                raise ValueError("apply_layer pairs must be disjoint")
+            used.update((i, i + 1))
+            pairs.append(self._prepare_pair(np.asarray(two_qudit[p]).reshape((self._qudit_dimension,) * 4),
+                                            i, i + 1, kwargs))
+        if self.track_norms:
+            for pr in pairs:
+                self._run_pairs([pr])
+                self._norms.append(self.norm())
+        else:
+            self._run_pairs(pairs)
+
+    def apply_layer_resident(self, one_qudit_dev, pair_left: Sequence[int], two_qudit_dev,
+                             maxsvals: Optional[int] = None, keep_left_canonical: bool = True) -> None:
+        """``apply_layer`` for gates already on the device (torch complex64:
+        one_qudit_dev (n, d, d), two_qudit_dev (p, d^2, d^2)).  Skips the
+        host-side unitarity and edge checks; shapes are still validated."""
+        d = self._qudit_dimension
+        if one_qudit_dev is not None:
+            if tuple(one_qudit_dev.shape) != (self._nqudits, d, d):
+                raise ValueError("one_qudit_dev must have shape (nqudits, d, d)")
+            lib = self._lib()
+            for i, site in enumerate(self._sites):
+                _native.check(lib.mps_apply_1q(
+                    self._stream(), ctypes.c_void_p(site.data_ptr()), int(site.shape[0]), d,
+                    int(site.shape[2]), ctypes.c_void_p(one_qudit_dev[i].data_ptr())))
+        if two_qudit_dev is None or len(pair_left) == 0:
+            return
+        used = set()
+        pairs = []
+        for p, i in enumerate(pair_left):
+            i = int(i)
+            if i in used or i + 1 in used or not (0 <= i < self._nqudits - 1):
+                raise ValueError("apply_layer_resident pairs must be disjoint and in range")
+            used.update((i, i + 1))
+            a, b = self._sites[i], self._sites[i + 1]
+            k = kept_count(maxsvals, min(int(a.shape[0]) * d, int(b.shape[2]) * d))
+            pairs.append((two_qudit_dev[p], i, k, bool(keep_left_canonical)))
+        self._run_pairs(pairs)
+
+    # -- shorthands (core.py:1278-1380) --------------------------------------
+    def x(self, index: int) -> None:
+        if index == -1:
+            self.apply_one_qudit_gate_to_all(xgate())
+        else:
+            self.apply_one_qudit_gate(xgate(), index)
+
+    def h(self, index: int) -> None:
+        if index == -1:
+            self.apply_one_qudit_gate_to_all(hgate())
+        else:
+            self.apply_one_qudit_gate(hgate(), index)
+
+    def r(self, index, seed: Optional[int] = None, angle_scale: float = 1.0) -> None:
+        if index == -1:
+            for i in range(self._nqudits):
+                self.apply_one_qudit_gate(rgate(seed, angle_scale), i)
+        else:
+            self.apply_one_qudit_gate(rgate(seed, angle_scale), index)
+
+    def cnot(self, a: int, b: int, **kwargs) -> None:
+        self.apply_two_qudit_gate(cnot(), a, b, **kwargs)
+
+    def haar_random(self, qudit1_index: int, qudit2_index: int, **kwargs) -> None:
+        gate = haar_random_unitary(nqudits=2, qudit_dimension=self._qudit_dimension)
+        self.apply_two_qudit_gate(gate, qudit1_index, qudit2_index, **kwargs)
+
+    def sweep_haar_random_left_to_right(self, **kwargs) -> None:
+        for i in range(0, self._nqudits - 1, 2):
+            self.haar_random(i, i + 1, keep_left_canonical=True, **kwargs)
+
+    def sweep_haar_random_right_to_left(self, **kwargs) -> None:
+        for i in range(self._nqudits - 2, 0, -2):
+            self.haar_random(i - 1, i, keep_left_canonical=False, **kwargs)
+
+    def sweep_cnots_left_to_right(self, **kwargs) -> None:
+        for i in range(0, self._nqudits - 1, 2):
+            self.cnot(i, i + 1, keep_left_canonical=True, **kwargs)
+
+    def sweep_cnots_right_to_left(self, **kwargs) -> None:
+        for i in range(self._nqudits - 2, 0, -2):
+            self.cnot(i - 1, i, keep_left_canonical=False, **kwargs)
+
+    def swap(self, a: int, b: int, **kwargs) -> None:
+        if b < a:
+            a, b = b, a
+        self.apply_two_qudit_gate(swap(), a, b, **kwargs)
+
+    # -- copies / comparison ---------------------------------------------
+    def copy(self) -> "MPS":
+        return self.__copy__()
+
+    def __copy__(self):
+        new = MPS.__new__(MPS)
+        new.__dict__.update(self.__dict__)
+        new._sites = [t.clone() for t in self._sites]
+        new._norms = list(self._norms)
+        new.svals_history = list(self.svals_history)
+        new.svd_params = _native.SvdParams(self.svd_params.max_sweeps, self.svd_params.tol,
+                                           self.svd_params.block_cols, 0)
+        return new
+
+    def __str__(self):
+        return "----".join(f"{self._prefix}{i}{tuple(t.shape)}" for i, t in enumerate(self._sites))
+
+    def __eq__(self, other):
+        if not isinstance(other, MPS):
+            return False
+        if self is other:
+            return True
+        if not self.is_valid():
+            raise ValueError("MPS is invalid and cannot be compared to another MPS.")
+        if not other.is_valid():
+            raise ValueError("Other MPS is invalid.")
+        if other._qudit_dimension != self._qudit_dimension or other._nqudits != self._nqudits:
+            return False
+        for a, b in zip(self._sites, other._sites):
+            if tuple(a.shape) != tuple(b.shape):
+                return False
+            if not np.allclose(a.cpu().numpy(), b.cpu().numpy()):
+                return False
+        return True
+
+    def __ne__(self, other):
+        return not self.__eq__(other)
+
+    __hash__ = None

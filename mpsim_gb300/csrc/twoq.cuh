@@ -1,0 +1,38 @@
+// Workspace geometry shared by the two-qudit kernels (merge, Jacobi SVD,
+// sort, regauge).  One slot per job; every job's slot has the same shape.
+//
+// For a job with theta of m x n (m = chi_l*d, n = d*chi_r):
+//   tall (m >= n): the Jacobi matrix X is theta itself, column-major,
+//                  C = n columns of length L = m.  X V = U S.
+//   wide (m <  n): X is theta^H (conjugate transpose), C = m columns of
+//                  length L = n.  theta = V S (X/S)^H.
+// X: lslot x cslot complex64, column-major (column c at X + c*lslot).
+// V: cslot x cslot complex64, column-major, starts as the identity.
+#pragma once
+
+#include "common.cuh"
+
+namespace mps {
+
+struct TwoQGeom {
+    int d;
+    int lslot;        // rows per slot, multiple of 32
+    int cslot;        // columns per slot, multiple of 32
+    cf* X;            // njobs * lslot * cslot
+    cf* V;            // njobs * cslot * cslot
+    float* sig;       // njobs * cslot: sorted singular values
+    int* perm;        // njobs * cslot: source column of each sorted value
+    float* offmax;    // njobs: max relative off-diagonal seen this sweep
+    int* done;        // njobs: 1 once a sweep made no rotation
+    int* need;        // njobs: kept columns that need an orthonormal completion
+    int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf
+};
+
+// Singular values at or below this (relative to max(s_0, 1)) are treated as
+// exact zeros: the isometric factor gets an orthonormal completion there.
+constexpr float kZeroSigma = 1e-30f;
+
+int merge_gate_launch(const mps_2q_job* jobs, int njobs, int max_chil, int max_chir,
+                      const TwoQGeom& g, cudaStream_t s);
+
+}  // namespace mps

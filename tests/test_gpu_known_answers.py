@@ -1,0 +1,349 @@
+"""Known-answer tests of the reference (mpsim/core_test.py) on the GPU path.
+
+Each test restates one of the reference's own tests against
+mpsim_gb300.MPS (which runs the sm_103a kernels through the C ABI); the
+expected values are the reference's.
+"""
+import copy as _copy
+
+import numpy as np
+import pytest
+
+import mpsim_gb300 as mpsim
+from mpsim_gb300 import MPS, MPSOperation
+from mpsim_gb300.gates import (cnot, computational_basis_projector, cphase, hgate, igate,
+                               one_state, plus_state, xgate, zero_state, zgate)
+from oracle.dense import DenseState
+from mpsim_gb300 import circuits as C
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _dev(cuda):
+    yield
+
+
+def test_product_states_and_bonds():                       # core_test.py:78-163, 358-367
+    for n in range(2, 8):
+        for d in (2, 3, 4):
+            mps = MPS(n, d)
+            assert mps.is_valid()
+            assert mps.bond_dimensions() == [1] * (n - 1)
+            wf = mps.wavefunction()
+            correct = np.zeros(d ** n)
+            correct[0] = 1
+            assert np.allclose(wf, correct)
+    assert MPS(5).max_bond_dimensions() == [2, 4, 4, 2]
+    assert MPS(8).max_bond_dimensions() == [2, 4, 8, 16, 8, 4, 2]
+    assert MPS(6, 10).max_bond_dimensions() == [10, 100, 1000, 100, 10]
+    assert MPS(4, 10).wavefunction().shape == (10 ** 4,)
+    m = MPS(10)
+    assert m.max_bond_dimension_of(-1) == 2 and m.max_bond_dimension_of(4) == 32
+
+
+@pytest.mark.parametrize("gate,expected", [(xgate(), one_state), (hgate(), plus_state),
+                                           (zgate(), zero_state), (igate(), zero_state)])
+def test_apply_one_qubit_gate(gate, expected):           # core_test.py:371-385
+    for n in range(2, 6):
+        for j in range(n):
+            mps = MPS(n)
+            mps.apply_one_qudit_gate(gate, j)
+            t = np.reshape(mps.get_node(j).tensor, (2,))
+            assert np.allclose(t, expected)
+
+
+def test_hadamard_all():                                   # core_test.py:398-406
+    mps = MPS(5)
+    mps.apply_one_qudit_gate_to_all(hgate())
+    assert np.allclose(mps.wavefunction(), np.ones(32) / 2 ** 2.5)
+
+
+def test_cnot_truth_table():                               # core_test.py:409-472
+    for pre, want in [((), 0), ((0,), 3), ((1,), 1), ((0, 1), 2)]:
+        mps = MPS(2)
+        for q in pre:
+            mps.x(q)
+        mps.apply_two_qudit_gate(cnot(), 0, 1)
+        c = np.zeros(4)
+        c[want] = 1
+        assert np.allclose(mps.wavefunction(), c)
+    for pre, want in [((0,), 2), ((), 0), ((1,), 3), ((0, 1), 1)]:
+        mps = MPS(2)
+        for q in pre:
+            mps.x(q)
+        mps.cnot(1, 0)
+        c = np.zeros(4)
+        c[want] = 1
+        assert np.allclose(mps.wavefunction(), c)
+
+
+def test_identical_indices_raise():                        # core_test.py:475-485
+    with pytest.raises(ValueError):
+        MPS(3).apply_two_qudit_gate(cnot(), 0, 0)
+
+
+@pytest.mark.parametrize("left", [True, False])
+def test_cnot_all_positions(left):                         # core_test.py:489-545
+    n = 5
+    for a in range(n - 1):
+        mps = MPS(n)
+        mps.x(a)
+        mps.cnot(a, a + 1, keep_left_canonical=left)
+        bits = ["0"] * n
+        bits[a] = bits[a + 1] = "1"
+        c = np.zeros(2 ** n)
+        c[int("".join(bits), 2)] = 1
+        assert np.allclose(mps.wavefunction(), c)
+
+
+@pytest.mark.parametrize("left", [True, False])
+def test_swap_and_hopping(left):                           # core_test.py:549-628, 888-902
+    mps = MPS(2)
+    mps.x(0)
+    mps.swap(0, 1, keep_left_canonical=left)
+    assert np.allclose(mps.wavefunction(), [0, 1, 0, 0])
+    n = 8
+    mps = MPS(n)
+    mps.h(0)
+    for i in range(1, n - 1):
+        mps.swap(i, i + 1, keep_left_canonical=left)
+    c = np.zeros(2 ** n)
+    c[0] = c[2 ** (n - 1)] = 2 ** -0.5
+    assert np.allclose(mps.wavefunction(), c)
+    for n in range(2, 12):
+        mps = MPS(n)
+        mps.x(0)
+        for i in range(n - 1):
+            mps.swap(i, i + 1, keep_left_canonical=True)
+        for i in range(n - 1, 0, -1):
+            mps.swap(i - 1, i, keep_left_canonical=True)
+        c = np.zeros(2 ** n)
+        c[2 ** (n - 1)] = 1
+        assert mps.is_valid() and np.allclose(mps.wavefunction(), c)
+
+
+def test_move_node_and_nonlocal():                         # core_test.py:631-771, 1225-1233
+    mps = MPS(10)
+    mps.x(0)
+    mps.move_node_from_left_to_right(0, 4)
+    c = np.zeros(2 ** 10)
+    c[2 ** 5] = 1
+    assert np.allclose(mps.wavefunction(), c)
+    with pytest.raises(ValueError):
+        MPS(5).move_node_from_left_to_right(current_node_index=4, final_node_index=0)
+    with pytest.raises(ValueError):
+        MPS(5).move_node_from_right_to_left(current_node_index=0, final_node_index=4)
+    for n in range(3, 9):
+        mps = MPS(n)
+        mps.x(0)
+        mps.cnot(0, n - 1)
+        c = np.zeros(2 ** n)
+        c[2 ** (n - 1) + 1] = 1
+        assert np.allclose(mps.wavefunction(), c)
+
+
+@pytest.mark.parametrize("left", [True, False])
+def test_bell_and_three_cnots(left):                       # core_test.py:773-873
+    mps = MPS(2)
+    mps.h(0)
+    mps.cnot(0, 1, keep_left_canonical=left)
+    assert np.allclose(mps.wavefunction(), np.array([1, 0, 0, 1]) / 2 ** 0.5)
+    for n in range(2, 9):
+        mps = MPS(n)
+        mps.x(0)
+        mps.cnot(0, 1, keep_left_canonical=left)
+        mps.h(-1)
+        mps.cnot(0, 1, keep_left_canonical=left)
+        mps.h(-1)
+        mps.cnot(0, 1)
+        c = np.zeros(2 ** n)
+        c[2 ** (n - 2)] = 1
+        assert np.allclose(mps.wavefunction(), c)
+
+
+def test_truncation_cases():                               # core_test.py:905-973, 1084-1101
+    mps = MPS(2)
+    mps.x(0)
+    mps.cnot(0, 1, max_singular_values=0.5)               # ignored keyword, as in the reference
+    assert np.allclose(mps.wavefunction(), [0, 0, 0, 1])
+    mps = MPS(2)
+    mps.h(0)
+    mps.cnot(0, 1, fraction=0.5)
+    assert np.allclose(mps.wavefunction(), [2 ** -0.5, 0, 0, 0])
+    mps = MPS(2)
+    mps.h(0)
+    mps.cnot(0, 1, fraction=1)
+    assert np.allclose(mps.wavefunction(), [2 ** -0.5, 0, 0, 2 ** -0.5])
+    mps = MPS(2)
+    mps.h(0)
+    mps.cnot(0, 1)
+    assert mps.bond_dimension_of(0) == 2
+    mps.cnot(0, 1)
+    assert mps.bond_dimension_of(0) == 2
+    mps = MPS(4)
+    mps.r(-1)
+    mps.apply_two_qudit_gate(cnot(), 0, 1, fraction=1)
+    assert mps.bond_dimensions() == [2, 1, 1]
+    mps = MPS(4)
+    mps.r(-1)
+    mps.apply_two_qudit_gate(cnot(), 0, 1, fraction=0.5)
+    assert mps.bond_dimensions() == [1, 1, 1]
+    mps = MPS(2)
+    mps.h(0)
+    mps.cnot(0, 1, maxsvals=1)
+    assert np.isclose(mps.norm(), 2 ** -0.5)
+    mps = MPS(2)
+    mps.h(0)
+    mps.cnot(0, 1, maxsvals=0)
+    assert mps.norm() == 0
+    with pytest.raises(ValueError):
+        MPS(2).cnot(0, 1, fraction=0.5, maxsvals=1)
+    with pytest.raises(ValueError):
+        MPS(2).cnot(0, 1, fraction=1.5)
+    with pytest.raises(TypeError):
+        MPS(2).cnot(0, 1, maxsvals=None)                  # int(None), as in the reference
+
+
+def test_inner_product_and_norm():                         # core_test.py:976-1081
+    states = []
+    for bits in [(), (1,), (0,), (0, 1)]:
+        m = MPS(2)
+        for q in bits:
+            m.apply(MPSOperation(xgate(), q))
+        states.append(m)
+    for i in range(4):
+        for j in range(4):
+            assert np.isclose(states[i].inner_product(states[j]), i == j)
+    with pytest.raises(ValueError):
+        MPS(5).inner_product(MPS(6))
+    with pytest.raises(ValueError):
+        MPS(5, 2).inner_product(MPS(5, 3))
+    for n in (3, 5, 8):
+        assert MPS(n).norm() == 1
+    for n in (2, 3, 5, 8):
+        a, b = C.brickwork(n, 4, seed=n), C.brickwork(n, 4, seed=100 + n)
+        ma, mb = MPS(n), MPS(n)
+        da, db = DenseState(n), DenseState(n)
+        for circ, m, ds in ((a, ma, da), (b, mb, db)):
+            for kind, sites, mat in circ.operations():
+                m.apply(MPSOperation(mpsim.gates.Node(mat.reshape((2,) * (2 * kind))), sites))
+                (ds.apply_one if kind == 1 else ds.apply_two)(mat, *sites)
+        want = np.inner(da.vector(), db.vector().conj())
+        assert np.isclose(ma.inner_product(mb), want, atol=1e-5)
+        assert np.isclose(mb.inner_product(ma), np.conj(want), atol=1e-5)
+
+
+def test_renormalize():                                    # core_test.py:1104-1185
+    for n in range(2, 6):
+        for d in (2, 3, 5):
+            mps = MPS(n, d)
+            mps.renormalize()
+            assert np.isclose(mps.norm(), 1.0)
+    mps = MPS(2)
+    mps.apply([MPSOperation(hgate(), (0,)), MPSOperation(cnot(), (0, 1))], maxsvals=1)
+    assert np.allclose(mps.wavefunction(), [2 ** -0.5, 0, 0, 0])
+    mps.renormalize()
+    assert np.allclose(mps.wavefunction(), [1, 0, 0, 0])
+    for norm in np.linspace(0.1, 2.0, 20):
+        mps.renormalize(to_norm=norm)
+        assert np.allclose(mps.wavefunction(), [norm, 0, 0, 0], atol=1e-6)
+        assert np.isclose(mps.norm(), norm)
+    z = MPS(2)
+    z.apply([MPSOperation(hgate(), (0,)), MPSOperation(cnot(), (0, 1))], maxsvals=0)
+    with pytest.raises(ValueError):
+        z.renormalize()
+    with pytest.raises(ValueError):
+        MPS(2).renormalize(to_norm=-3.14)
+    with pytest.raises(ValueError):
+        MPS(2).renormalize(to_norm=1e-20)
+
+
+def test_ghz_qft_nonlocal():                               # core_test.py:1236-1258
+    for n in range(3, 8):
+        mps = MPS(n)
+        mps.h(0)
+        for i in range(1, n):
+            mps.cnot(0, i)
+        c = np.zeros(2 ** n)
+        c[0] = c[-1] = 2 ** -0.5
+        assert np.allclose(mps.wavefunction(), c)
+    for n in range(3, 8):
+        mps = MPS(n)
+        for i in range(n - 1, -1, -1):
+            mps.h(i)
+            for j in range(i - 1, -1, -1):
+                mps.apply_two_qudit_gate(cphase(2 ** (j - i)), j, i)
+        assert np.allclose(mps.wavefunction(), np.ones(2 ** n) / 2 ** (n / 2))
+
+
+@pytest.mark.parametrize("chi", [16, 32, 64, 128])
+def test_max_bond_dimension_not_surpassed(chi):            # core_test.py:1471-1497
+    rng = np.random.default_rng(chi)
+    n = 10
+    mps = MPS(n)
+    singles = (hgate(), xgate(), zgate())
+    cz = cphase(0.5)
+    for _ in range(6):
+        for i in range(n):
+            mps.apply(MPSOperation(singles[rng.integers(3)], (i,)))
+        for i in range(n):
+            j = int(rng.choice([q for q in range(n) if q != i]))
+            mps.apply(MPSOperation(cz, (i, j)), maxsvals=chi)
+        assert all(b <= chi for b in mps.bond_dimensions())
+
+
+def test_equal_copy_expectation_dagger():                  # core_test.py:1500-1585
+    for n in (2, 3, 5):
+        for d in (2, 3):
+            m1, m2 = MPS(n, d), MPS(n, d)
+            assert m1 == m2
+            if d == 2:
+                m1.apply(MPSOperation(xgate(), 0))
+                assert m1 != m2
+                m2.apply(MPSOperation(xgate(), 0))
+                assert m1 == m2
+            c = _copy.copy(m1)
+            assert c is not m1 and c == m1
+    assert MPS(4, tensor_prefix="a") == MPS(4, tensor_prefix="b")
+    mps = MPS(2)
+    h0 = MPSOperation(hgate(), 0)
+    assert np.isclose(mps.expectation(h0), 2 ** -0.5)
+    assert np.isclose(mps.expectation(MPSOperation(xgate(), 0)), 0.0)
+    mps.apply(MPSOperation(xgate(), 0))
+    assert np.isclose(mps.expectation(h0), -(2 ** -0.5))
+    m = MPS(3)
+    m.apply_one_qudit_gate(C.haar_random_matrix(1, 2, 4), 0)
+    m.cnot(0, 1)
+    wf = m.wavefunction()
+    m.dagger()
+    assert np.allclose(m.wavefunction(), wf.conj())
+
+
+def test_povm_without_ortho():                             # core_test.py:1288-1338
+    pi0 = computational_basis_projector(state=0)
+    mps = MPS(3)
+    mps.apply([MPSOperation(hgate(), i) for i in range(3)])
+    mps.apply_one_qudit_gate(pi0, 0, ortho_after_non_unitary=False,
+                             renormalize_after_non_unitary=False)
+    assert np.isclose(mps.norm(), 2 ** -0.5)
+    assert np.allclose(mps.wavefunction(), 2 ** -1.5 * np.array([1] * 4 + [0] * 4))
+
+
+def test_known_answer_fixture(cuda):
+    """Cases run through the reference itself (tests/golden/known_answers.npz)."""
+    import os
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "known_answers.npz"))
+    m = MPS(4, 3)
+    for i in range(4):
+        m.apply_one_qudit_gate(C.haar_random_matrix(1, 3, 11 + i), i)
+    for (a, b) in [(0, 1), (2, 3), (1, 2), (2, 1), (0, 1)]:
+        g = C.haar_random_matrix(2, 3, 100 + a * 7 + b).reshape(3, 3, 3, 3)
+        m.apply_two_qudit_gate(mpsim.gates.Node(g), a, b, keep_left_canonical=(a != 2))
+    assert np.allclose(m.wavefunction(), z["qutrit4_mixed"], atol=1e-5)
+    m = MPS(5)
+    m.h(0)
+    for i in range(1, 5):
+        m.cnot(0, i)
+    assert np.allclose(m.wavefunction(), z["ghz5_nonlocal"], atol=1e-6)
