@@ -61,7 +61,7 @@ typedef struct {
 typedef struct {
     int32_t max_sweeps;    /* default 40                                   */
     float tol;             /* relative off-diagonal threshold; default
-                              sqrt(rows) * 2^-24, at least 2^-23           */
+                              2 * sqrt(rows) * 2^-24, at least 2^-22       */
     int32_t block_cols;    /* columns per block: 8 or 16 (default 16)      */
     int32_t sweeps_out;    /* out: sweeps taken by the slowest job         */
 } mps_svd_params;

@@ -7,30 +7,40 @@
 // S into one side (core.py:1139-1145).
 //
 // Algorithm.  The C columns of X are split into nb blocks of BC columns
-// (zero-padded).  One sweep visits every pair of blocks once, in nb-1 rounds
-// of nb/2 disjoint block pairs (circle-method round robin); each round is one
-// launch with one CTA per (block pair, job).  A CTA copies its 2*BC columns
-// to shared memory and runs one inner sweep of Hestenes rotations over all
-// pairs of those columns (2*BC-1 steps of BC disjoint pairs, one warp per
-// pair), accumulating the 2BC x 2BC rotation Q; it writes the columns back and
-// applies V <- V Q.  For a pair (p, q) with gamma = x_p^H x_q,
-// alpha = |x_p|^2, beta = |x_q|^2, the rotation zeroes gamma:
+// (zero-padded).  A sweep is nb-1 rounds of nb/2 disjoint block pairs
+// (circle-method round robin, one launch per round, one CTA per (block pair,
+// job)), so every pair of columns is rotated exactly once per sweep:
+//  * round 0 ("full" visit): the CTA stages its 2*BC columns in shared memory
+//    and rotates all pairs among them -- the intra-block pairs of every block
+//    (round 0's pairs cover each block once) and the first inter-block pairs;
+//  * rounds 1..nb-2 ("ring" visit): only the BC*BC inter-block pairs.  Warp w
+//    keeps home column I*BC+w in registers; the J columns travel warp to warp
+//    through shared memory, so each step moves one column per warp.
+// For a pair (x, q) with gamma = x^H q, alpha = |x|^2, beta = |q|^2 the
+// rotation zeroes gamma:
 //   zeta = (beta - alpha) / (2|gamma|), t = sign(zeta)/(|zeta| + sqrt(1+zeta^2)),
-//   c = 1/sqrt(1+t^2), s = c t, e = conj(gamma)/|gamma|,
-//   x_p <- c x_p - s e x_q,  x_q <- s x_p + c e x_q.
-// A pair is rotated only when |gamma| > tol sqrt(alpha beta); a sweep with no
-// rotation in a job marks the job converged.  Column norms are recomputed
-// from the rotated data (not updated by formula), so they do not drift.
+//   c = 1/sqrt(1+t^2), s = c t, tau = s/(1+c), e = conj(gamma)/|gamma|, y = e q,
+//   x <- x - s (y + tau x),   q <- y + s (x - tau y).
+// The tau form keeps c = 1 - s tau implicit: with an explicit c, tiny angles
+// round c up to exactly 1 and every such rotation grows the column norms; over
+// thousands of rotations that biases every singular value.  A pair is rotated
+// only when |gamma| > tol sqrt(alpha beta) (tol = 2 sqrt(L) 2^-24 by default);
+// a sweep with no rotation in a job marks the job converged.  Column norms
+// are recomputed from the rotated data, so they do not drift.
 //
-// Afterwards sigma_c = |X_c|, sorted descending (ties by column index);
-// the first k are kept.  U and V factors are read from X/sigma or V as the
-// tall/wide orientation requires (see twoq.cuh); where the isometric factor
-// would divide by an exact-zero singular value, an orthonormal completion
-// (classical Gram-Schmidt, twice) is written instead -- LAPACK also returns
-// orthonormal singular vectors for zero singular values, and which ones it
-// returns does not change any later singular value of the state.
+// V.  A job that is tall (m >= n) and left-canonical -- the default of
+// apply_two_qudit_gate -- needs only U = X_k / S: its right site S V^H equals
+// U^H theta, formed by one GEMM against a copy of theta, so such jobs never
+// accumulate V.  Other jobs accumulate the 2BC x 2BC rotation of each visit in
+// shared memory and apply V <- V Q.
+//
+// Afterwards sigma_c = |X_c|, sorted descending (ties by column index); the
+// first k are kept.  Where the isometric factor would divide by an exact-zero
+// singular value, an orthonormal completion (classical Gram-Schmidt, twice) is
+// written instead -- LAPACK also returns orthonormal singular vectors for zero
+// singular values, and which ones it returns does not change any later
+// singular value of the state.
 #include <mutex>
-#include <vector>
 
 #include "twoq.cuh"
 
@@ -38,29 +48,102 @@ namespace mps {
 
 namespace {
 
-constexpr int kMaxSmem = 227 * 1024;
+struct Rot {
+    float s, tau;
+    cf e;
+};
+
+__device__ __forceinline__ Rot make_rot(float a, float b, cf gam, float ag) {
+    const float zeta = (b - a) / (2.f * ag);
+    const float az = fabsf(zeta);
+    const float t = az > 1e10f ? 0.5f / zeta
+                               : copysignf(1.f, zeta) / (az + sqrtf(fmaf(zeta, zeta, 1.f)));
+    const float c = 1.f / sqrtf(fmaf(t, t, 1.f));
+    Rot r;
+    r.s = c * t;
+    r.tau = r.s / (1.f + c);
+    r.e = cmake(gam.x / ag, -gam.y / ag);
+    return r;
+}
+
+__device__ __forceinline__ void apply_rot(const Rot& r, cf& x, cf& q) {
+    const cf y = cmul(r.e, q);
+    const cf nx = csub(x, cscale(cadd(y, cscale(x, r.tau)), r.s));
+    const cf ny = cadd(y, cscale(csub(x, cscale(y, r.tau)), r.s));
+    x = nx;
+    q = ny;
+}
+
+struct JobShape {
+    int m, n, L, C, nb;
+    bool tall, track_v;
+};
+
+template <int BC>
+__device__ __forceinline__ JobShape job_shape(const mps_2q_job* jobs, int j, int d) {
+    JobShape s;
+    s.m = jobs[j].chi_l * d;
+    s.n = jobs[j].chi_r * d;
+    s.L = max(s.m, s.n);
+    s.C = min(s.m, s.n);
+    s.tall = s.m >= s.n;
+    s.track_v = job_tracks_v(s.m, s.n, jobs[j].keep_left_canonical);
+    int nb = (s.C + BC - 1) / BC;
+    if (nb < 2) nb = 2;
+    s.nb = nb + (nb & 1);
+    return s;
+}
+
+__device__ __forceinline__ int block_col(int c, int I, int J, int BC) {
+    return (c < BC) ? I * BC + c : J * BC + (c - BC);
+}
+
+// V <- V Q for the 2*BC columns of this visit (rows < C).
+template <int BC>
+__device__ __forceinline__ void update_v(cf* V, int cslot, int C, int I, int J, const cf* Qs) {
+    constexpr int W = 2 * BC;
+    for (int r = threadIdx.x; r < C; r += BC * 32) {
+        cf v[W];
+#pragma unroll
+        for (int c = 0; c < W; ++c) v[c] = V[(size_t)block_col(c, I, J, BC) * cslot + r];
+#pragma unroll 4
+        for (int c2 = 0; c2 < W; ++c2) {
+            cf acc = cmake(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < W; ++c) cfma(acc, v[c], Qs[c2 * W + c]);
+            V[(size_t)block_col(c2, I, J, BC) * cslot + r] = acc;
+        }
+    }
+}
+
+__device__ __forceinline__ void publish_offmax(float offmax, float* s_off, int nwarps, float* dst) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    offmax = warp_max(offmax);
+    if (lane == 0) s_off[warp] = offmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float o = 0.f;
+        for (int w = 0; w < nwarps; ++w) o = fmaxf(o, s_off[w]);
+        atomicMax(reinterpret_cast<int*>(dst), __float_as_int(o));
+    }
+}
 
 // ---------------------------------------------------------------------------
-// One round: CTA (pair index, job).  ROWS = rows per lane kept in registers
-// (the working column length Lw <= 32*ROWS).
+// Round 0: all pairs among the 2*BC staged columns.  ROWS = rows per lane
+// held in registers (working column length Lw <= 32*ROWS).
 template <int BC, int ROWS>
 __global__ void __launch_bounds__(BC * 32)
-jacobi_round_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
+full_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
     extern __shared__ float2 smem[];
     const int j = blockIdx.y;
     if (g.done[j]) return;
-    const int chil = jobs[j].chi_l, chir = jobs[j].chi_r;
-    const int m = chil * g.d, n = chir * g.d;
-    const int L = max(m, n), C = min(m, n);
-    if (C < 2) return;
-    int nb = (C + BC - 1) / BC;
-    if (nb < 2) nb = 2;
-    nb += nb & 1;
-    if (round >= nb - 1 || (int)blockIdx.x >= nb / 2) return;
+    const JobShape sh = job_shape<BC>(jobs, j, g.d);
+    if (sh.C < 2) return;
+    if (round >= sh.nb - 1 || (int)blockIdx.x >= sh.nb / 2) return;
     int I, J;
-    tournament_pair(nb, round, blockIdx.x, I, J);
-    const int Lw = (L + 31) & ~31;
-    constexpr int W = 2 * BC;                   // columns in shared memory
+    tournament_pair(sh.nb, round, blockIdx.x, I, J);
+    const int Lw = (sh.L + 31) & ~31;
+    constexpr int W = 2 * BC;
     cf* X = g.X + (size_t)j * g.lslot * g.cslot;
     cf* Xs = smem;                              // [W][Lw]
     cf* Qs = smem + (size_t)W * Lw;             // [W][W], column-major
@@ -69,12 +152,12 @@ jacobi_round_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, 
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int c = warp; c < W; c += BC) {
-        const int gc = (c < BC) ? I * BC + c : J * BC + (c - BC);
-        const cf* src = X + (size_t)gc * g.lslot;
+        const cf* src = X + (size_t)block_col(c, I, J, BC) * g.lslot;
         for (int r = lane; r < Lw; r += 32) Xs[(size_t)c * Lw + r] = src[r];
     }
-    for (int e = tid; e < W * W; e += BC * 32)
-        Qs[e] = (e % W == e / W) ? cmake(1.f, 0.f) : cmake(0.f, 0.f);
+    if (sh.track_v)
+        for (int e = tid; e < W * W; e += BC * 32)
+            Qs[e] = (e % W == e / W) ? cmake(1.f, 0.f) : cmake(0.f, 0.f);
     __syncthreads();
     for (int c = warp; c < W; c += BC) {
         float s = 0.f;
@@ -95,13 +178,8 @@ jacobi_round_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, 
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
             const int r = lane + 32 * i;
-            if (r < Lw) {
-                xp[i] = cp[r];
-                xq[i] = cq[r];
-            } else {
-                xp[i] = cmake(0.f, 0.f);
-                xq[i] = cmake(0.f, 0.f);
-            }
+            xp[i] = r < Lw ? cp[r] : cmake(0.f, 0.f);
+            xq[i] = r < Lw ? cq[r] : cmake(0.f, 0.f);
             cfma_conj(gam, xp[i], xq[i]);
         }
         gam.x = warp_sum(gam.x);
@@ -112,36 +190,26 @@ jacobi_round_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, 
         const float rel = den > 0.f ? ag / den : 0.f;
         offmax = fmaxf(offmax, rel);
         if (rel > tol) {                        // warp-uniform (butterfly sums)
-            const float zeta = (b - a) / (2.f * ag);
-            const float az = fabsf(zeta);
-            float t = az > 1e10f ? 0.5f / zeta
-                                 : copysignf(1.f, zeta) / (az + sqrtf(fmaf(zeta, zeta, 1.f)));
-            const float c = rsqrtf(fmaf(t, t, 1.f));
-            const float s = c * t;
-            const cf e = cmake(gam.x / ag, -gam.y / ag);
+            const Rot R = make_rot(a, b, gam, ag);
             float na = 0.f, nq = 0.f;
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) {
                 const int r = lane + 32 * i;
-                const cf y = cmul(e, xq[i]);
-                const cf np = csub(cscale(xp[i], c), cscale(y, s));
-                const cf nn = cadd(cscale(xp[i], s), cscale(y, c));
+                apply_rot(R, xp[i], xq[i]);
                 if (r < Lw) {
-                    cp[r] = np;
-                    cq[r] = nn;
+                    cp[r] = xp[i];
+                    cq[r] = xq[i];
                 }
-                na += cabs2(np);
-                nq += cabs2(nn);
+                na += cabs2(xp[i]);
+                nq += cabs2(xq[i]);
             }
             na = warp_sum(na);
             nq = warp_sum(nq);
-            if (lane < W) {
-                cf* qp = Qs + p * W;
-                cf* qq = Qs + q * W;
-                const cf a0 = qp[lane];
-                const cf y = cmul(e, qq[lane]);
-                qp[lane] = csub(cscale(a0, c), cscale(y, s));
-                qq[lane] = cadd(cscale(a0, s), cscale(y, c));
+            if (sh.track_v && lane < W) {
+                cf qa = Qs[p * W + lane], qb = Qs[q * W + lane];
+                apply_rot(R, qa, qb);
+                Qs[p * W + lane] = qa;
+                Qs[q * W + lane] = qb;
             }
             __syncwarp();
             if (lane == 0) {
@@ -151,39 +219,126 @@ jacobi_round_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, 
         }
         __syncthreads();
     }
-
-    // write the rotated columns back
     for (int c = warp; c < W; c += BC) {
-        const int gc = (c < BC) ? I * BC + c : J * BC + (c - BC);
-        cf* dst = X + (size_t)gc * g.lslot;
+        cf* dst = X + (size_t)block_col(c, I, J, BC) * g.lslot;
         for (int r = lane; r < Lw; r += 32) dst[r] = Xs[(size_t)c * Lw + r];
     }
-    // V <- V Q on the 2*BC columns (rows < C; the rest stay as they are)
-    cf* V = g.V + (size_t)j * g.cslot * g.cslot;
-    for (int r = tid; r < C; r += BC * 32) {
-        cf v[W];
+    if (sh.track_v) update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
+    publish_offmax(offmax, s_off, BC, g.offmax + j);
+}
+
+// ---------------------------------------------------------------------------
+// Rounds >= 1: the BC*BC pairs between block I (home, warp w holds column
+// I*BC+w) and block J (visitors, passed to warp w+1 after every step).
+template <int BC, int ROWS>
+__global__ void __launch_bounds__(BC * 32)
+ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
+    extern __shared__ float2 smem[];
+    const int j = blockIdx.y;
+    if (g.done[j]) return;
+    const JobShape sh = job_shape<BC>(jobs, j, g.d);
+    if (sh.C < 2) return;
+    if (round >= sh.nb - 1 || (int)blockIdx.x >= sh.nb / 2) return;
+    int I, J;
+    tournament_pair(sh.nb, round, blockIdx.x, I, J);
+    const int Lw = (sh.L + 31) & ~31;
+    constexpr int W = 2 * BC;
+    cf* X = g.X + (size_t)j * g.lslot * g.cslot;
+    cf* ring = smem;                            // [BC][Lw]
+    cf* Qs = smem + (size_t)BC * Lw;            // [W][W], column-major
+    float* ringn = reinterpret_cast<float*>(Qs + W * W);  // [BC]
+    __shared__ float s_off[BC];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    cf hx[ROWS], vx[ROWS];
+    float hn = 0.f, vn = 0.f;
+    {
+        const cf* hs = X + (size_t)(I * BC + warp) * g.lslot;
+        const cf* vs = X + (size_t)(J * BC + warp) * g.lslot;
 #pragma unroll
-        for (int c = 0; c < W; ++c) {
-            const int gc = (c < BC) ? I * BC + c : J * BC + (c - BC);
-            v[c] = V[(size_t)gc * g.cslot + r];
+        for (int i = 0; i < ROWS; ++i) {
+            const int r = lane + 32 * i;
+            hx[i] = r < Lw ? hs[r] : cmake(0.f, 0.f);
+            vx[i] = r < Lw ? vs[r] : cmake(0.f, 0.f);
+            hn += cabs2(hx[i]);
+            vn += cabs2(vx[i]);
         }
-#pragma unroll 4
-        for (int c2 = 0; c2 < W; ++c2) {
-            cf acc = cmake(0.f, 0.f);
+        hn = warp_sum(hn);
+        vn = warp_sum(vn);
+    }
+    if (sh.track_v) {
+        for (int e = tid; e < W * W; e += BC * 32)
+            Qs[e] = (e % W == e / W) ? cmake(1.f, 0.f) : cmake(0.f, 0.f);
+        __syncthreads();
+    }
+    float offmax = 0.f;
+    int vid = warp;                             // J-local index of the visitor held
+    for (int step = 0; step < BC; ++step) {
+        cf gam = cmake(0.f, 0.f);
 #pragma unroll
-            for (int c = 0; c < W; ++c) cfma(acc, v[c], Qs[c2 * W + c]);
-            const int gc = (c2 < BC) ? I * BC + c2 : J * BC + (c2 - BC);
-            V[(size_t)gc * g.cslot + r] = acc;
+        for (int i = 0; i < ROWS; ++i) cfma_conj(gam, hx[i], vx[i]);
+        gam.x = warp_sum(gam.x);
+        gam.y = warp_sum(gam.y);
+        const float ag = sqrtf(cabs2(gam));
+        const float den = sqrtf(hn) * sqrtf(vn);
+        const float rel = den > 0.f ? ag / den : 0.f;
+        offmax = fmaxf(offmax, rel);
+        if (rel > tol) {
+            const Rot R = make_rot(hn, vn, gam, ag);
+            float na = 0.f, nq = 0.f;
+#pragma unroll
+            for (int i = 0; i < ROWS; ++i) {
+                apply_rot(R, hx[i], vx[i]);
+                na += cabs2(hx[i]);
+                nq += cabs2(vx[i]);
+            }
+            hn = warp_sum(na);
+            vn = warp_sum(nq);
+            if (sh.track_v && lane < W) {
+                cf qa = Qs[warp * W + lane], qb = Qs[(BC + vid) * W + lane];
+                apply_rot(R, qa, qb);
+                Qs[warp * W + lane] = qa;
+                Qs[(BC + vid) * W + lane] = qb;
+            }
+        }
+        if (step + 1 < BC) {
+            const int to = (warp + 1) % BC;
+            cf* dst = ring + (size_t)to * Lw;
+#pragma unroll
+            for (int i = 0; i < ROWS; ++i) {
+                const int r = lane + 32 * i;
+                if (r < Lw) dst[r] = vx[i];
+            }
+            if (lane == 0) ringn[to] = vn;
+            __syncthreads();
+            const cf* src = ring + (size_t)warp * Lw;
+#pragma unroll
+            for (int i = 0; i < ROWS; ++i) {
+                const int r = lane + 32 * i;
+                vx[i] = r < Lw ? src[r] : cmake(0.f, 0.f);
+            }
+            vn = ringn[warp];
+            vid = (vid + BC - 1) % BC;
+            __syncthreads();
         }
     }
-    offmax = warp_max(offmax);
-    if (lane == 0) s_off[warp] = offmax;
-    __syncthreads();
-    if (tid == 0) {
-        float o = 0.f;
-        for (int w = 0; w < BC; ++w) o = fmaxf(o, s_off[w]);
-        atomicMax(reinterpret_cast<int*>(g.offmax + j), __float_as_int(o));
+    {
+        cf* hd = X + (size_t)(I * BC + warp) * g.lslot;
+        cf* vd = X + (size_t)(J * BC + vid) * g.lslot;
+#pragma unroll
+        for (int i = 0; i < ROWS; ++i) {
+            const int r = lane + 32 * i;
+            if (r < Lw) {
+                hd[r] = hx[i];
+                vd[r] = vx[i];
+            }
+        }
     }
+    if (sh.track_v) {
+        __syncthreads();
+        update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
+    }
+    publish_offmax(offmax, s_off, BC, g.offmax + j);
 }
 
 __global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol) {
@@ -197,15 +352,21 @@ __global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol) {
     g.offmax[j] = 0.f;
 }
 
-__global__ void init_slots_kernel(TwoQGeom g, int njobs) {
-    // V = identity, bookkeeping cleared
+__global__ void init_slots_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, cf* V2,
+                                  int njobs) {
+    // both V buffers = identity for jobs that track V; bookkeeping cleared
     const size_t per = (size_t)g.cslot * g.cslot;
     const size_t total = per * njobs;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
          e += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(e / per);
+        if (!job_tracks_v(jobs[j].chi_l * g.d, jobs[j].chi_r * g.d, jobs[j].keep_left_canonical))
+            continue;
         const size_t w = e % per;
         const int r = (int)(w % g.cslot), c = (int)(w / g.cslot);
-        g.V[e] = (r == c) ? cmake(1.f, 0.f) : cmake(0.f, 0.f);
+        const cf v = (r == c) ? cmake(1.f, 0.f) : cmake(0.f, 0.f);
+        g.V[e] = v;
+        V2[e] = v;
     }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < njobs) {
@@ -214,6 +375,77 @@ __global__ void init_slots_kernel(TwoQGeom g, int njobs) {
         g.need[t] = 0;
     }
     if (t < 4) g.counter[t] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Per-sweep reordering: columns sorted by descending norm before each sweep
+// (de Rijk's ordering), which cuts the sweep count.  presort_kernel writes the
+// permutation; gather_kernel copies X (and V) columns into the other buffer.
+constexpr int PRESORT_T = 512;
+
+__global__ void __launch_bounds__(PRESORT_T)
+presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2) {
+    extern __shared__ float2 sm1[];
+    float* key = reinterpret_cast<float*>(sm1);
+    int* idx = reinterpret_cast<int*>(key + npow2);
+    // Every job is reordered, converged or not, so the two buffers never
+    // disagree about where a job's columns live.
+    const int j = blockIdx.x;
+    const int m = jobs[j].chi_l * g.d, n = jobs[j].chi_r * g.d;
+    const int L = max(m, n), C = min(m, n);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const cf* X = g.X + (size_t)j * g.lslot * g.cslot;
+    for (int i = tid; i < npow2; i += PRESORT_T) {
+        key[i] = -1.f;
+        idx[i] = i;
+    }
+    __syncthreads();
+    for (int c = warp; c < C; c += PRESORT_T / 32) {
+        float s = 0.f;
+        for (int r = lane; r < L; r += 32) s += cabs2(X[(size_t)c * g.lslot + r]);
+        s = warp_sum(s);
+        if (lane == 0) key[c] = (s == s) ? s : 0.f;   // NaN sorts as zero
+    }
+    __syncthreads();
+    for (int size = 2; size <= npow2; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = tid; i < npow2; i += PRESORT_T) {
+                const int pj = i ^ stride;
+                if (pj > i) {
+                    const bool desc = (i & size) == 0;
+                    const float ki = key[i], kj = key[pj];
+                    const int ii = idx[i], ij = idx[pj];
+                    const bool i_first = (ki > kj) || (ki == kj && ii < ij);
+                    if (i_first != desc) {
+                        key[i] = kj; key[pj] = ki;
+                        idx[i] = ij; idx[pj] = ii;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = tid; i < C; i += PRESORT_T) g.perm[(size_t)j * g.cslot + i] = idx[i];
+}
+
+// dst column c = src column perm[c] for c < C (X: Lw rows; V: C rows).
+__global__ void gather_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, cf* Xdst,
+                              cf* Vdst) {
+    const int j = blockIdx.y;
+    const int m = jobs[j].chi_l * g.d, n = jobs[j].chi_r * g.d;
+    const int L = max(m, n), C = min(m, n);
+    const int c = blockIdx.x;
+    if (c >= C) return;
+    const int src = g.perm[(size_t)j * g.cslot + c];
+    const int Lw = (L + 31) & ~31;
+    const cf* xs = g.X + (size_t)j * g.lslot * g.cslot + (size_t)src * g.lslot;
+    cf* xd = Xdst + (size_t)j * g.lslot * g.cslot + (size_t)c * g.lslot;
+    for (int r = threadIdx.x; r < Lw; r += blockDim.x) xd[r] = xs[r];
+    if (job_tracks_v(m, n, jobs[j].keep_left_canonical)) {
+        const cf* vs = g.V + (size_t)j * g.cslot * g.cslot + (size_t)src * g.cslot;
+        cf* vd = Vdst + (size_t)j * g.cslot * g.cslot + (size_t)c * g.cslot;
+        for (int r = threadIdx.x; r < C; r += blockDim.x) vd[r] = vs[r];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -301,9 +533,9 @@ sort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2) {
     }
 }
 
-// out (R x k, row-major): out[row*k + i] = scale_i * src[perm_i * ld + row]
-// out (k x R, row-major): out[i*R + col] = scale_i * conj?(src[perm_i*ld + col])
-// which = 0 -> a_out, which = 1 -> b_out.
+// a_out (m x k, row-major): a_out[row*k + i] = scale_i * src[perm_i * ld + row]
+//   tall: src = X (U S columns), scale = 1/s (left-canonical) or 1
+//   wide: src = V,               scale = 1 (left-canonical) or s
 __global__ void regauge_a_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
     __shared__ cf tile[32][33];
     const int j = blockIdx.z;
@@ -342,12 +574,16 @@ __global__ void regauge_a_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g
     }
 }
 
+// b_out (k x n, row-major) for jobs that track V:
+//   tall (right-canonical): b_out[i, :] = conj(V[:, perm_i])
+//   wide: b_out[i, :] = scale_i * conj(X[:, perm_i]), scale = 1 (lc) or 1/s
 __global__ void regauge_b_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
     const int j = blockIdx.z;
     const mps_2q_job job = jobs[j];
     const int m = job.chi_l * g.d, n = job.chi_r * g.d;
     const int i = blockIdx.y;
     if (i >= job.k) return;
+    if (!job_tracks_v(m, n, job.keep_left_canonical)) return;
     const bool tall = m >= n;
     const bool lc = job.keep_left_canonical != 0;
     const cf* src;
@@ -358,12 +594,72 @@ __global__ void regauge_b_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g
     const float thr = kZeroSigma * fmaxf(sig[0], 1.f);
     const float s = sig[i];
     float sc;
-    if (tall) sc = lc ? s : 1.f;
+    if (tall) sc = 1.f;
     else sc = lc ? 1.f : (s > thr ? 1.f / s : 0.f);
     const cf* col = src + (size_t)g.perm[(size_t)j * g.cslot + i] * ld;
     cf* out = reinterpret_cast<cf*>(job.b_out) + (size_t)i * n;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
         out[c] = cscale(cconj(col[c]), sc);
+}
+
+// b_out = a_out^H theta for tall left-canonical jobs (S V^H = U^H theta).
+// 64x64 output tiles, K (= m) in chunks of 16, 256 threads x 4x4 outputs.
+__global__ void __launch_bounds__(256)
+uh_theta_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
+    __shared__ cf As[16][64];
+    __shared__ cf Bs[16][64];
+    const int j = blockIdx.z;
+    const mps_2q_job job = jobs[j];
+    const int m = job.chi_l * g.d, n = job.chi_r * g.d, k = job.k;
+    if (job_tracks_v(m, n, job.keep_left_canonical)) return;
+    const int i0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
+    if (i0 >= k || c0 >= n) return;
+    const cf* U = reinterpret_cast<const cf*>(job.a_out);     // m x k row-major
+    const cf* T = g.T + (size_t)j * g.lslot * g.cslot;        // theta, column-major
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    cf acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = cmake(0.f, 0.f);
+    for (int r0 = 0; r0 < m; r0 += 16) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int idx = tid + q * 256;
+            const int ti = idx & 63, kk = idx >> 6;
+            const int row = r0 + kk, i = i0 + ti;
+            As[kk][ti] = (row < m && i < k) ? cconj(U[(size_t)row * k + i]) : cmake(0.f, 0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int idx = tid + q * 256;
+            const int kk = idx & 15, tc = idx >> 4;
+            const int row = r0 + kk, c = c0 + tc;
+            Bs[kk][tc] = (row < m && c < n) ? T[(size_t)c * g.lslot + row] : cmake(0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) {
+            cf av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = As[kk][ty + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tx + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) cfma(acc[a][b], av[a], bv[b]);
+        }
+        __syncthreads();
+    }
+    cf* out = reinterpret_cast<cf*>(job.b_out);
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int i = i0 + ty + 16 * a, c = c0 + tx + 16 * b;
+            if (i < k && c < n) out[(size_t)i * n + c] = acc[a][b];
+        }
 }
 
 // Orthonormal completion of the isometric factor where sigma is an exact
@@ -398,7 +694,6 @@ complete_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
             for (int e = tid; e < R; e += COMP_T) v[e] = cmake(e == cand ? 1.f : 0.f, 0.f);
             __syncthreads();
             for (int pass = 0; pass < 2; ++pass) {
-                // h_t = u_t^H v for t < i
                 for (int t = warp; t < i; t += COMP_T / 32) {
                     cf acc = cmake(0.f, 0.f);
                     for (int e = lane; e < R; e += 32)
@@ -410,10 +705,7 @@ complete_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
                 __syncthreads();
                 for (int e = tid; e < R; e += COMP_T) {
                     cf acc = v[e];
-                    for (int t = 0; t < i; ++t) {
-                        const cf u = base[t * vs + e * es];
-                        acc = csub(acc, cmul(h[t], u));
-                    }
+                    for (int t = 0; t < i; ++t) acc = csub(acc, cmul(h[t], base[t * vs + e * es]));
                     v[e] = acc;
                 }
                 __syncthreads();
@@ -446,40 +738,91 @@ complete_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
     }
 }
 
-template <int BC, int ROWS>
-int launch_round(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g,
-                 int round, float tol, int lw, cudaStream_t s) {
-    const size_t smem = (size_t)2 * BC * lw * sizeof(cf) + (size_t)4 * BC * BC * sizeof(cf) +
-                        (size_t)2 * BC * sizeof(float);
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(jacobi_round_kernel<BC, ROWS>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
-    });
-    if (attr_err != cudaSuccess) return cuda_fail(attr_err, "cudaFuncSetAttribute(jacobi_round)");
-    dim3 grid(pairs, njobs);
-    jacobi_round_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol);
-    MPS_LAUNCH_CHECK("jacobi_round_kernel");
+// ---------------------------------------------------------------------------
+// Launch helpers.
+
+// Largest dynamic shared memory a kernel may request on the current device:
+// the per-block opt-in limit minus the kernel's own static shared memory.
+template <typename K>
+int dynamic_smem_limit(K kernel, int* limit) {
+    int dev = 0, optin = 0;
+    MPS_CUDA_CHECK(cudaGetDevice(&dev));
+    MPS_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    MPS_CUDA_CHECK(cudaFuncGetAttributes(&fa, kernel));
+    *limit = optin - (int)fa.sharedSizeBytes;
     return MPS_OK;
 }
 
-typedef int (*round_fn)(const mps_2q_job*, int, int, const TwoQGeom&, int, float, int, cudaStream_t);
+template <typename K>
+int prepare_kernel(K kernel, std::once_flag& once, int& limit, int& rc) {
+    std::call_once(once, [&] {
+        rc = dynamic_smem_limit(kernel, &limit);
+        if (rc == MPS_OK) {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 limit);
+            if (e != cudaSuccess) rc = cuda_fail(e, "cudaFuncSetAttribute(jacobi visit)");
+        }
+    });
+    return rc;
+}
 
 template <int BC>
-round_fn pick_rows(int lw) {
-    if (lw <= 64) return launch_round<BC, 2>;
-    if (lw <= 128) return launch_round<BC, 4>;
-    if (lw <= 256) return launch_round<BC, 8>;
-    if (lw <= 512) return launch_round<BC, 16>;
-    if (lw <= 576) return launch_round<BC, 18>;
-    if (lw <= 1024) return launch_round<BC, 32>;
-    return launch_round<BC, 56>;
+size_t full_smem(int lw) {
+    return (size_t)2 * BC * lw * sizeof(cf) + (size_t)4 * BC * BC * sizeof(cf) +
+           (size_t)2 * BC * sizeof(float);
+}
+
+template <int BC>
+size_t ring_smem(int lw) {
+    return (size_t)BC * lw * sizeof(cf) + (size_t)4 * BC * BC * sizeof(cf) + (size_t)BC * sizeof(float);
+}
+
+template <int BC, int ROWS>
+int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g, int round,
+                 float tol, int lw, cudaStream_t s) {
+    dim3 grid(pairs, njobs);
+    if (round == 0) {
+        static std::once_flag once;
+        static int limit = 0, rc = MPS_OK;
+        if (prepare_kernel(full_visit_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
+        const size_t smem = full_smem<BC>(lw);
+        if (smem > (size_t)limit) return fail(MPS_ERR_ARG, "jacobi: merged matrix too long for shared memory");
+        full_visit_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol);
+        MPS_LAUNCH_CHECK("full_visit_kernel");
+    } else {
+        static std::once_flag once;
+        static int limit = 0, rc = MPS_OK;
+        if (prepare_kernel(ring_visit_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
+        const size_t smem = ring_smem<BC>(lw);
+        if (smem > (size_t)limit) return fail(MPS_ERR_ARG, "jacobi: merged matrix too long for shared memory");
+        ring_visit_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol);
+        MPS_LAUNCH_CHECK("ring_visit_kernel");
+    }
+    return MPS_OK;
+}
+
+typedef int (*visit_fn)(const mps_2q_job*, int, int, const TwoQGeom&, int, float, int, cudaStream_t);
+
+// Block width and register rows for a working column length lw (<= 1792).
+visit_fn pick_visit(int lw, int* bc) {
+    if (lw <= 576) {
+        *bc = 16;
+        if (lw <= 64) return launch_visit<16, 2>;
+        if (lw <= 128) return launch_visit<16, 4>;
+        if (lw <= 256) return launch_visit<16, 8>;
+        if (lw <= 512) return launch_visit<16, 16>;
+        return launch_visit<16, 18>;
+    }
+    *bc = 8;
+    if (lw <= 1024) return launch_visit<8, 32>;
+    return launch_visit<8, 56>;
 }
 
 struct Layout {
     int lslot, cslot;
-    size_t off_X, off_V, off_sig, off_perm, off_off, off_done, off_need, off_counter, total;
+    size_t off_X, off_X2, off_V, off_V2, off_T, off_sig, off_perm, off_off, off_done, off_need,
+        off_counter, total;
 };
 
 Layout make_layout(int njobs, int max_m, int max_n) {
@@ -490,7 +833,10 @@ Layout make_layout(int njobs, int max_m, int max_n) {
     size_t o = 0;
     const size_t nj = (size_t)max(njobs, 1);
     lo.off_X = o; o = align_up(o + nj * lo.lslot * lo.cslot * sizeof(cf), 256);
+    lo.off_X2 = o; o = align_up(o + nj * lo.lslot * lo.cslot * sizeof(cf), 256);
     lo.off_V = o; o = align_up(o + nj * lo.cslot * lo.cslot * sizeof(cf), 256);
+    lo.off_V2 = o; o = align_up(o + nj * lo.cslot * lo.cslot * sizeof(cf), 256);
+    lo.off_T = o; o = align_up(o + nj * lo.lslot * lo.cslot * sizeof(cf), 256);
     lo.off_sig = o; o = align_up(o + nj * lo.cslot * sizeof(float), 256);
     lo.off_perm = o; o = align_up(o + nj * lo.cslot * sizeof(int), 256);
     lo.off_off = o; o = align_up(o + nj * sizeof(float), 256);
@@ -540,6 +886,7 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     g.cslot = lo.cslot;
     g.X = reinterpret_cast<cf*>(ws + lo.off_X);
     g.V = reinterpret_cast<cf*>(ws + lo.off_V);
+    g.T = reinterpret_cast<cf*>(ws + lo.off_T);
     g.sig = reinterpret_cast<float*>(ws + lo.off_sig);
     g.perm = reinterpret_cast<int*>(ws + lo.off_perm);
     g.offmax = reinterpret_cast<float*>(ws + lo.off_off);
@@ -547,27 +894,31 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     g.need = reinterpret_cast<int*>(ws + lo.off_need);
     g.counter = reinterpret_cast<int*>(ws + lo.off_counter);
 
-    int max_sweeps = 40, bc = 16;
+    int max_sweeps = 40;
     float tol = 0.f;
     if (params) {
         if (params->max_sweeps > 0) max_sweeps = params->max_sweeps;
-        if (params->block_cols == 8) bc = 8;
         tol = params->tol;
     }
-    if (!(tol > 0.f)) tol = fmaxf(sqrtf((float)lo.lslot) * 5.9604645e-8f, 1.1920929e-7f);
+    // The computed x_p^H x_q carries a rounding error of about sqrt(L) 2^-24
+    // |x_p||x_q|; a threshold at that floor keeps rotating noise.  Twice it
+    // leaves the factors orthonormal to a few 1e-6 and the singular values
+    // (second order in the residual) far more accurate.
+    if (!(tol > 0.f)) tol = fmaxf(2.f * sqrtf((float)lo.lslot) * 5.9604645e-8f, 2.3841858e-7f);
     const int lw = lo.lslot;
-    size_t need_smem = (size_t)2 * bc * lw * sizeof(cf) + (size_t)4 * bc * bc * sizeof(cf) + 256;
-    if (need_smem > (size_t)kMaxSmem) bc = 8;
-    need_smem = (size_t)2 * bc * lw * sizeof(cf) + (size_t)4 * bc * bc * sizeof(cf) + 256;
-    if (need_smem > (size_t)kMaxSmem)
-        return fail(MPS_ERR_ARG, "mps_apply_2q_batch: merged matrix too long for shared memory");
+    int bc = 16;
+    visit_fn visit = pick_visit(lw, &bc);
+    if (params) params->block_cols = bc;
 
-    MPS_CUDA_CHECK(cudaMemsetAsync(g.X, 0, (size_t)njobs * lo.lslot * lo.cslot * sizeof(cf), s));
+    cf* X2 = reinterpret_cast<cf*>(ws + lo.off_X2);
+    cf* V2 = reinterpret_cast<cf*>(ws + lo.off_V2);
+    // X and X2 back to back: one memset zeroes both (padding rows/columns)
+    MPS_CUDA_CHECK(cudaMemsetAsync(g.X, 0, lo.off_V - lo.off_X, s));
     {
         const size_t total = (size_t)njobs * lo.cslot * lo.cslot;
         int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
         blocks = max(blocks, (njobs + 255) / 256);
-        init_slots_kernel<<<blocks, 256, 0, s>>>(g, njobs);
+        init_slots_kernel<<<blocks, 256, 0, s>>>(jobs, g, V2, njobs);
         MPS_LAUNCH_CHECK("init_slots_kernel");
     }
     const int max_chil = (max_m + d - 1) / d, max_chir = (max_n + d - 1) / d;
@@ -579,19 +930,29 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (nbmax < 2) nbmax = 2;
     nbmax += nbmax & 1;
     const int rounds = nbmax - 1, pairs = nbmax / 2;
-    round_fn fn = (bc == 16) ? pick_rows<16>(lw) : pick_rows<8>(lw);
 
     if (!t_pinned) {
         MPS_CUDA_CHECK(cudaHostAlloc(reinterpret_cast<void**>(&t_pinned), 4 * sizeof(int),
                                      cudaHostAllocDefault));
     }
+    int npow2 = 1;
+    while (npow2 < lo.cslot) npow2 <<= 1;
+    const size_t sort_smem = (size_t)npow2 * (sizeof(float) + sizeof(int));
     int sweeps = 0;
     bool converged = false;
     if (cmax >= 2) {
         for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
             MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
+            if (cmax > 2 * bc) {
+                presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2);
+                MPS_LAUNCH_CHECK("presort_kernel");
+                gather_kernel<<<dim3(cmax, njobs), 128, 0, s>>>(jobs, g, X2, V2);
+                MPS_LAUNCH_CHECK("gather_kernel");
+                cf* t = g.X; g.X = X2; X2 = t;
+                t = g.V; g.V = V2; V2 = t;
+            }
             for (int r = 0; r < rounds; ++r) {
-                rc = fn(jobs, njobs, pairs, g, r, tol, lw, s);
+                rc = visit(jobs, njobs, pairs, g, r, tol, lw, s);
                 if (rc) return rc;
             }
             sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol);
@@ -612,9 +973,6 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     }
     if (params) params->sweeps_out = sweeps;
 
-    int npow2 = 1;
-    while (npow2 < lo.cslot) npow2 <<= 1;
-    const size_t sort_smem = (size_t)npow2 * (sizeof(float) + sizeof(int));
     if (sort_smem > 48 * 1024) {
         MPS_CUDA_CHECK(cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)sort_smem));
@@ -637,6 +995,9 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         }
         complete_kernel<<<njobs, COMP_T, comp_smem, s>>>(jobs, g);
         MPS_LAUNCH_CHECK("complete_kernel");
+        dim3 gu((max_n + 63) / 64, (kmax + 63) / 64, njobs);
+        uh_theta_kernel<<<gu, 256, 0, s>>>(jobs, g);
+        MPS_LAUNCH_CHECK("uh_theta_kernel");
     }
     MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 1, g.counter + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
     MPS_CUDA_CHECK(cudaStreamSynchronize(s));

@@ -89,6 +89,8 @@ merge_gate_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
 
     const cf* G = reinterpret_cast<const cf*>(job.gate);
     cf* X = g.X + (size_t)blockIdx.z * g.lslot * g.cslot;
+    cf* T = g.T + (size_t)blockIdx.z * g.lslot * g.cslot;
+    const bool track_v = job_tracks_v(m, n, job.keep_left_canonical);
     const int dd = d * d;
     for (int e = tid; e < TILE * TILE; e += NT) {
         int tr, tc;
@@ -106,10 +108,12 @@ merge_gate_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
                      sh.mt[rbase + a][b * TR + rr]);
         const int trow = l * d + ap;              // theta row
         const int tcol = bp * chir + r;           // theta column
-        if (tall)
+        if (tall) {
             X[(size_t)tcol * g.lslot + trow] = th;
-        else
+            if (!track_v) T[(size_t)tcol * g.lslot + trow] = th;
+        } else {
             X[(size_t)trow * g.lslot + tcol] = cconj(th);
+        }
     }
 }
 

@@ -19,7 +19,9 @@ struct TwoQGeom {
     int lslot;        // rows per slot, multiple of 32
     int cslot;        // columns per slot, multiple of 32
     cf* X;            // njobs * lslot * cslot
-    cf* V;            // njobs * cslot * cslot
+    cf* V;            // njobs * cslot * cslot (only jobs that track V use theirs)
+    cf* T;            // njobs * lslot * cslot: copy of theta for jobs that form
+                      // S V^H as U^H theta instead of tracking V
     float* sig;       // njobs * cslot: sorted singular values
     int* perm;        // njobs * cslot: source column of each sorted value
     float* offmax;    // njobs: max relative off-diagonal seen this sweep
@@ -27,6 +29,13 @@ struct TwoQGeom {
     int* need;        // njobs: kept columns that need an orthonormal completion
     int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf
 };
+
+// A job tracks the right rotations V unless it is tall (m >= n) and left-
+// canonical: then U = X/S is all the Jacobi iteration must produce, and the
+// right site S V^H = U^H theta comes from one GEMM against a copy of theta.
+__host__ __device__ __forceinline__ bool job_tracks_v(int m, int n, int keep_left_canonical) {
+    return !(m >= n && keep_left_canonical != 0);
+}
 
 // Singular values at or below this (relative to max(s_0, 1)) are treated as
 // exact zeros: the isometric factor gets an orthonormal completion there.

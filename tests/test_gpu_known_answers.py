@@ -18,6 +18,20 @@ from mpsim_gb300 import circuits as C
 
 pytestmark = pytest.mark.gpu
 
+# The reference's tests use np.allclose defaults (atol 1e-8); the reference
+# meets that because its float64 cnot/swap and complex128 gates promote the
+# whole state to complex128.  This build stores complex64, whose rounding is
+# ~6e-8, so the ported assertions use atol 1e-6 (rtol stays 1e-5).
+_allclose = np.allclose
+
+
+def close(a, b, **kw):
+    kw.setdefault("atol", 1e-6)
+    return _allclose(a, b, **kw)
+
+
+np_allclose_default_atol = 1e-8
+
 
 @pytest.fixture(autouse=True)
 def _dev(cuda):
@@ -33,7 +47,7 @@ def test_product_states_and_bonds():                       # core_test.py:78-163
             wf = mps.wavefunction()
             correct = np.zeros(d ** n)
             correct[0] = 1
-            assert np.allclose(wf, correct)
+            assert close(wf, correct)
     assert MPS(5).max_bond_dimensions() == [2, 4, 4, 2]
     assert MPS(8).max_bond_dimensions() == [2, 4, 8, 16, 8, 4, 2]
     assert MPS(6, 10).max_bond_dimensions() == [10, 100, 1000, 100, 10]
@@ -50,13 +64,13 @@ def test_apply_one_qubit_gate(gate, expected):           # core_test.py:371-385
             mps = MPS(n)
             mps.apply_one_qudit_gate(gate, j)
             t = np.reshape(mps.get_node(j).tensor, (2,))
-            assert np.allclose(t, expected)
+            assert close(t, expected)
 
 
 def test_hadamard_all():                                   # core_test.py:398-406
     mps = MPS(5)
     mps.apply_one_qudit_gate_to_all(hgate())
-    assert np.allclose(mps.wavefunction(), np.ones(32) / 2 ** 2.5)
+    assert close(mps.wavefunction(), np.ones(32) / 2 ** 2.5)
 
 
 def test_cnot_truth_table():                               # core_test.py:409-472
@@ -67,7 +81,7 @@ def test_cnot_truth_table():                               # core_test.py:409-47
         mps.apply_two_qudit_gate(cnot(), 0, 1)
         c = np.zeros(4)
         c[want] = 1
-        assert np.allclose(mps.wavefunction(), c)
+        assert close(mps.wavefunction(), c)
     for pre, want in [((0,), 2), ((), 0), ((1,), 3), ((0, 1), 1)]:
         mps = MPS(2)
         for q in pre:
@@ -75,7 +89,7 @@ def test_cnot_truth_table():                               # core_test.py:409-47
         mps.cnot(1, 0)
         c = np.zeros(4)
         c[want] = 1
-        assert np.allclose(mps.wavefunction(), c)
+        assert close(mps.wavefunction(), c)
 
 
 def test_identical_indices_raise():                        # core_test.py:475-485
@@ -94,7 +108,7 @@ def test_cnot_all_positions(left):                         # core_test.py:489-54
         bits[a] = bits[a + 1] = "1"
         c = np.zeros(2 ** n)
         c[int("".join(bits), 2)] = 1
-        assert np.allclose(mps.wavefunction(), c)
+        assert close(mps.wavefunction(), c)
 
 
 @pytest.mark.parametrize("left", [True, False])
@@ -102,7 +116,7 @@ def test_swap_and_hopping(left):                           # core_test.py:549-62
     mps = MPS(2)
     mps.x(0)
     mps.swap(0, 1, keep_left_canonical=left)
-    assert np.allclose(mps.wavefunction(), [0, 1, 0, 0])
+    assert close(mps.wavefunction(), [0, 1, 0, 0])
     n = 8
     mps = MPS(n)
     mps.h(0)
@@ -110,7 +124,7 @@ def test_swap_and_hopping(left):                           # core_test.py:549-62
         mps.swap(i, i + 1, keep_left_canonical=left)
     c = np.zeros(2 ** n)
     c[0] = c[2 ** (n - 1)] = 2 ** -0.5
-    assert np.allclose(mps.wavefunction(), c)
+    assert close(mps.wavefunction(), c)
     for n in range(2, 12):
         mps = MPS(n)
         mps.x(0)
@@ -120,7 +134,7 @@ def test_swap_and_hopping(left):                           # core_test.py:549-62
             mps.swap(i - 1, i, keep_left_canonical=True)
         c = np.zeros(2 ** n)
         c[2 ** (n - 1)] = 1
-        assert mps.is_valid() and np.allclose(mps.wavefunction(), c)
+        assert mps.is_valid() and close(mps.wavefunction(), c)
 
 
 def test_move_node_and_nonlocal():                         # core_test.py:631-771, 1225-1233
@@ -129,7 +143,7 @@ def test_move_node_and_nonlocal():                         # core_test.py:631-77
     mps.move_node_from_left_to_right(0, 4)
     c = np.zeros(2 ** 10)
     c[2 ** 5] = 1
-    assert np.allclose(mps.wavefunction(), c)
+    assert close(mps.wavefunction(), c)
     with pytest.raises(ValueError):
         MPS(5).move_node_from_left_to_right(current_node_index=4, final_node_index=0)
     with pytest.raises(ValueError):
@@ -140,7 +154,7 @@ def test_move_node_and_nonlocal():                         # core_test.py:631-77
         mps.cnot(0, n - 1)
         c = np.zeros(2 ** n)
         c[2 ** (n - 1) + 1] = 1
-        assert np.allclose(mps.wavefunction(), c)
+        assert close(mps.wavefunction(), c)
 
 
 @pytest.mark.parametrize("left", [True, False])
@@ -148,7 +162,7 @@ def test_bell_and_three_cnots(left):                       # core_test.py:773-87
     mps = MPS(2)
     mps.h(0)
     mps.cnot(0, 1, keep_left_canonical=left)
-    assert np.allclose(mps.wavefunction(), np.array([1, 0, 0, 1]) / 2 ** 0.5)
+    assert close(mps.wavefunction(), np.array([1, 0, 0, 1]) / 2 ** 0.5)
     for n in range(2, 9):
         mps = MPS(n)
         mps.x(0)
@@ -159,22 +173,22 @@ def test_bell_and_three_cnots(left):                       # core_test.py:773-87
         mps.cnot(0, 1)
         c = np.zeros(2 ** n)
         c[2 ** (n - 2)] = 1
-        assert np.allclose(mps.wavefunction(), c)
+        assert close(mps.wavefunction(), c)
 
 
 def test_truncation_cases():                               # core_test.py:905-973, 1084-1101
     mps = MPS(2)
     mps.x(0)
     mps.cnot(0, 1, max_singular_values=0.5)               # ignored keyword, as in the reference
-    assert np.allclose(mps.wavefunction(), [0, 0, 0, 1])
+    assert close(mps.wavefunction(), [0, 0, 0, 1])
     mps = MPS(2)
     mps.h(0)
     mps.cnot(0, 1, fraction=0.5)
-    assert np.allclose(mps.wavefunction(), [2 ** -0.5, 0, 0, 0])
+    assert close(mps.wavefunction(), [2 ** -0.5, 0, 0, 0])
     mps = MPS(2)
     mps.h(0)
     mps.cnot(0, 1, fraction=1)
-    assert np.allclose(mps.wavefunction(), [2 ** -0.5, 0, 0, 2 ** -0.5])
+    assert close(mps.wavefunction(), [2 ** -0.5, 0, 0, 2 ** -0.5])
     mps = MPS(2)
     mps.h(0)
     mps.cnot(0, 1)
@@ -242,12 +256,12 @@ def test_renormalize():                                    # core_test.py:1104-1
             assert np.isclose(mps.norm(), 1.0)
     mps = MPS(2)
     mps.apply([MPSOperation(hgate(), (0,)), MPSOperation(cnot(), (0, 1))], maxsvals=1)
-    assert np.allclose(mps.wavefunction(), [2 ** -0.5, 0, 0, 0])
+    assert close(mps.wavefunction(), [2 ** -0.5, 0, 0, 0])
     mps.renormalize()
-    assert np.allclose(mps.wavefunction(), [1, 0, 0, 0])
+    assert close(mps.wavefunction(), [1, 0, 0, 0])
     for norm in np.linspace(0.1, 2.0, 20):
         mps.renormalize(to_norm=norm)
-        assert np.allclose(mps.wavefunction(), [norm, 0, 0, 0], atol=1e-6)
+        assert close(mps.wavefunction(), [norm, 0, 0, 0], atol=1e-6)
         assert np.isclose(mps.norm(), norm)
     z = MPS(2)
     z.apply([MPSOperation(hgate(), (0,)), MPSOperation(cnot(), (0, 1))], maxsvals=0)
@@ -267,14 +281,14 @@ def test_ghz_qft_nonlocal():                               # core_test.py:1236-1
             mps.cnot(0, i)
         c = np.zeros(2 ** n)
         c[0] = c[-1] = 2 ** -0.5
-        assert np.allclose(mps.wavefunction(), c)
+        assert close(mps.wavefunction(), c)
     for n in range(3, 8):
         mps = MPS(n)
         for i in range(n - 1, -1, -1):
             mps.h(i)
             for j in range(i - 1, -1, -1):
                 mps.apply_two_qudit_gate(cphase(2 ** (j - i)), j, i)
-        assert np.allclose(mps.wavefunction(), np.ones(2 ** n) / 2 ** (n / 2))
+        assert close(mps.wavefunction(), np.ones(2 ** n) / 2 ** (n / 2))
 
 
 @pytest.mark.parametrize("chi", [16, 32, 64, 128])
@@ -317,7 +331,7 @@ def test_equal_copy_expectation_dagger():                  # core_test.py:1500-1
     m.cnot(0, 1)
     wf = m.wavefunction()
     m.dagger()
-    assert np.allclose(m.wavefunction(), wf.conj())
+    assert close(m.wavefunction(), wf.conj())
 
 
 def test_povm_without_ortho():                             # core_test.py:1288-1338
@@ -327,7 +341,7 @@ def test_povm_without_ortho():                             # core_test.py:1288-1
     mps.apply_one_qudit_gate(pi0, 0, ortho_after_non_unitary=False,
                              renormalize_after_non_unitary=False)
     assert np.isclose(mps.norm(), 2 ** -0.5)
-    assert np.allclose(mps.wavefunction(), 2 ** -1.5 * np.array([1] * 4 + [0] * 4))
+    assert close(mps.wavefunction(), 2 ** -1.5 * np.array([1] * 4 + [0] * 4))
 
 
 def test_known_answer_fixture(cuda):
@@ -341,9 +355,9 @@ def test_known_answer_fixture(cuda):
     for (a, b) in [(0, 1), (2, 3), (1, 2), (2, 1), (0, 1)]:
         g = C.haar_random_matrix(2, 3, 100 + a * 7 + b).reshape(3, 3, 3, 3)
         m.apply_two_qudit_gate(mpsim.gates.Node(g), a, b, keep_left_canonical=(a != 2))
-    assert np.allclose(m.wavefunction(), z["qutrit4_mixed"], atol=1e-5)
+    assert close(m.wavefunction(), z["qutrit4_mixed"], atol=1e-5)
     m = MPS(5)
     m.h(0)
     for i in range(1, 5):
         m.cnot(0, i)
-    assert np.allclose(m.wavefunction(), z["ghz5_nonlocal"], atol=1e-6)
+    assert close(m.wavefunction(), z["ghz5_nonlocal"], atol=1e-6)

@@ -4,7 +4,8 @@ Each job merges random sites with a Haar gate; the kernel's singular values,
 truncated two-site block, isometry of the canonical factor and discarded
 weight are compared with an SVD of the same merged matrix in complex128.
 Tolerances (complex64 arithmetic): singular values |s - s_ref| <=
-2e-5 s_ref + 2e-6 s_ref[0]; truncated block and isometry to 2e-5 relative.
+2e-5 s_ref + 2e-6 s_ref[0]; isometry to 2e-5; truncated block to
+max(2e-5, 3x the error of LAPACK's complex64 SVD on the same input).
 """
 import ctypes
 
@@ -99,8 +100,15 @@ def check_job(spec, out, d):
     best = (u[:, :k] * s[:k]) @ vh[:k]
     gap_ok = k == len(s) or s[k - 1] - s[k] > 1e-3 * s0
     if gap_ok:
-        err = np.linalg.norm(left @ right - best) / max(np.linalg.norm(best), 1e-30)
-        assert err < 2e-5, err
+        # Truncating at a spectral gap amplifies any complex64 SVD's rounding
+        # by about s0/gap; the bar is 3x what LAPACK's complex64 SVD of the
+        # same (complex64-rounded) theta achieves, and never below 2e-5.
+        u4, s4, vh4 = np.linalg.svd(th.astype(np.complex64), full_matrices=False)
+        lap = ((u4[:, :k] * s4[:k]) @ vh4[:k]).astype(np.complex128)
+        nb = max(np.linalg.norm(best), 1e-30)
+        lap_err = np.linalg.norm(lap - best) / nb
+        err = np.linalg.norm(left @ right - best) / nb
+        assert err < max(2e-5, 3 * lap_err), (err, lap_err)
     iso = left if lc else right.T
     gram = iso.conj().T @ iso if lc else right @ right.conj().T
     assert np.allclose(gram, np.eye(k), atol=2e-5), np.max(np.abs(gram - np.eye(k)))
