@@ -95,6 +95,24 @@ int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs_dev, int njobs,
                        int max_m, int max_n, int d, void* workspace,
                        size_t workspace_bytes, mps_svd_params* params);
 
+/* Size of the fixed device scratch array behind mps_apply_2q_batch_noalloc. */
+#define MPS_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* mps_apply_2q_batch for callers that cannot allocate device memory (an
+ * application whose own pool owns the GPU's memory, a plugin host that gives
+ * its plugins no allocator, a loop that must never enter the allocator).
+ * No counterpart in the reference (it has no native interface at all).
+ * Same jobs, same results; scratch comes from a static __device__ array of
+ * MPS_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * exit, and the call allocates nothing.  Jobs whose slots need more scratch
+ * than that are rejected with MPS_ERR_WORKSPACE (at theta 512x512 about three
+ * jobs fit per call).  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current: make it before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs_dev, int njobs,
+                               int max_m, int max_n, int d, mps_svd_params* params);
+
 /* Workspace bytes for the contractions below (sites of at most max_chi). */
 size_t mps_sweep_workspace_bytes(int max_chi, int d);
 

@@ -21,6 +21,7 @@ MPS_ERR_CUDA = 2
 MPS_ERR_WORKSPACE = 3
 MPS_ERR_NOT_CONVERGED = 4
 MPS_ERR_NONFINITE = 5
+NOALLOC_SCRATCH_BYTES = 32 << 20       # MPS_NOALLOC_SCRATCH_BYTES
 
 STATUS_NOT_CONVERGED = 1
 STATUS_NONFINITE = 2
@@ -52,6 +53,7 @@ SIGNATURES = {
     "mps_apply_1q": (_I, [_P, _P, _I, _I, _I, _P]),
     "mps_2q_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
     "mps_apply_2q_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _SZ, ctypes.POINTER(SvdParams)]),
+    "mps_apply_2q_batch_noalloc": (_I, [_P, _P, _I, _I, _I, _I, ctypes.POINTER(SvdParams)]),
     "mps_sweep_workspace_bytes": (_SZ, [_I, _I]),
     "mps_inner_product": (_I, [_P, _P, _P, _P, _P, _I, _I, _P, _SZ, _P]),
     "mps_wavefunction": (_I, [_P, _P, _P, _I, _I, _P, _P, _SZ]),

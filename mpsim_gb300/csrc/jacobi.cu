@@ -41,6 +41,7 @@
 // singular values, and which ones it returns does not change any later
 // singular value of the state.
 #include <mutex>
+#include <string>
 
 #include "twoq.cuh"
 
@@ -1004,5 +1005,197 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (t_pinned[1] != 0) return fail(MPS_ERR_NONFINITE, "mps_apply_2q_batch: NaN/Inf singular value");
     if (!converged)
         return fail(MPS_ERR_NOT_CONVERGED, "mps_apply_2q_batch: Jacobi SVD hit its sweep cap");
+    return MPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of mps_apply_2q_batch.
+//
+// Some callers cannot allocate device memory: an application whose memory
+// pool owns the whole GPU and forbids allocations outside it, a plugin host
+// that hands its plugins no allocator, or a latency-critical loop that must
+// never enter the allocator.  This entry point takes its scratch from the
+// fixed array below instead of from a caller-provided workspace, and makes
+// no allocation of its own (no cudaMalloc/cudaFree, no pinned host buffer:
+// the per-sweep convergence count is read into a stack variable).
+//
+// The array is a static __device__ object: every GPU that loads this library
+// holds MPS_NOALLOC_SCRATCH_BYTES of it until the process exits.  In host code
+// its name is only a host-side stand-in, never a device address; the device
+// address is looked up with cudaGetSymbolAddress once per device, with that
+// device current, on the first call made on that device -- so make that first
+// call before any stream capture.  All calls share the one array and it keeps
+// the previous call's contents: the driver clears everything that must start
+// at zero, and calls that overlap on the GPU (two streams, two threads) race
+// on it and must be serialised by the caller.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MPS_NOALLOC_SCRATCH_BYTES];
+
+namespace mps {
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::once_flag g_noalloc_once[kMaxDevices];
+void* g_noalloc_ptr[kMaxDevices];
+cudaError_t g_noalloc_err[kMaxDevices];
+
+int noalloc_scratch(void** ptr) {
+    int dev = 0;
+    MPS_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(MPS_ERR_ARG, "mps_apply_2q_batch_noalloc: device index out of range");
+    std::call_once(g_noalloc_once[dev], [dev] {
+        g_noalloc_err[dev] = cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch);
+    });
+    if (g_noalloc_err[dev] != cudaSuccess)
+        return cuda_fail(g_noalloc_err[dev], "cudaGetSymbolAddress(g_noalloc_scratch)");
+    *ptr = g_noalloc_ptr[dev];
+    return MPS_OK;
+}
+
+}  // namespace
+}  // namespace mps
+
+extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, int njobs,
+                                          int max_m, int max_n, int d,
+                                          mps_svd_params* params) {
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (njobs == 0) return MPS_OK;
+    if (njobs < 0 || njobs > 65535 || !jobs)
+        return fail(MPS_ERR_ARG, "mps_apply_2q_batch_noalloc: bad job list");
+    if (d < 1 || d > 64) return fail(MPS_ERR_ARG, "mps_apply_2q_batch_noalloc: qudit dimension must be 1..64");
+    if (max_m <= 0 || max_n <= 0)
+        return fail(MPS_ERR_ARG, "mps_apply_2q_batch_noalloc: max_m/max_n must be positive");
+    const Layout lo = make_layout(njobs, max_m, max_n);
+    if (lo.lslot > 1792)
+        return fail(MPS_ERR_ARG, "mps_apply_2q_batch_noalloc: merged matrix longer than 1792 rows "
+                                 "is beyond this build's shared-memory Jacobi kernel");
+    if (lo.total > (size_t)MPS_NOALLOC_SCRATCH_BYTES)
+        return fail(MPS_ERR_WORKSPACE,
+                    "mps_apply_2q_batch_noalloc: these jobs need " + std::to_string(lo.total) +
+                        " bytes of scratch, more than the fixed " +
+                        std::to_string((size_t)MPS_NOALLOC_SCRATCH_BYTES) +
+                        "; use mps_apply_2q_batch with a workspace, or fewer/smaller jobs per call");
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+
+    char* ws = static_cast<char*>(scratch);
+    TwoQGeom g;
+    g.d = d;
+    g.lslot = lo.lslot;
+    g.cslot = lo.cslot;
+    g.X = reinterpret_cast<cf*>(ws + lo.off_X);
+    g.V = reinterpret_cast<cf*>(ws + lo.off_V);
+    g.T = reinterpret_cast<cf*>(ws + lo.off_T);
+    g.sig = reinterpret_cast<float*>(ws + lo.off_sig);
+    g.perm = reinterpret_cast<int*>(ws + lo.off_perm);
+    g.offmax = reinterpret_cast<float*>(ws + lo.off_off);
+    g.done = reinterpret_cast<int*>(ws + lo.off_done);
+    g.need = reinterpret_cast<int*>(ws + lo.off_need);
+    g.counter = reinterpret_cast<int*>(ws + lo.off_counter);
+
+    int max_sweeps = 40;
+    float tol = 0.f;
+    if (params) {
+        if (params->max_sweeps > 0) max_sweeps = params->max_sweeps;
+        tol = params->tol;
+    }
+    if (!(tol > 0.f)) tol = fmaxf(2.f * sqrtf((float)lo.lslot) * 5.9604645e-8f, 2.3841858e-7f);
+    const int lw = lo.lslot;
+    int bc = 16;
+    visit_fn visit = pick_visit(lw, &bc);
+    if (params) params->block_cols = bc;
+
+    cf* X2 = reinterpret_cast<cf*>(ws + lo.off_X2);
+    cf* V2 = reinterpret_cast<cf*>(ws + lo.off_V2);
+    // the array keeps the last call's contents: clear X, X2 (padding must be
+    // zero), set V/V2 to I and reset the per-job flags and counters
+    MPS_CUDA_CHECK(cudaMemsetAsync(g.X, 0, lo.off_V - lo.off_X, s));
+    {
+        const size_t total = (size_t)njobs * lo.cslot * lo.cslot;
+        int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+        blocks = max(blocks, (njobs + 255) / 256);
+        init_slots_kernel<<<blocks, 256, 0, s>>>(jobs, g, V2, njobs);
+        MPS_LAUNCH_CHECK("init_slots_kernel");
+    }
+    const int max_chil = (max_m + d - 1) / d, max_chir = (max_n + d - 1) / d;
+    rc = merge_gate_launch(jobs, njobs, max_chil, max_chir, g, s);
+    if (rc) return rc;
+
+    const int cmax = min(max_m, max_n);
+    int nbmax = (cmax + bc - 1) / bc;
+    if (nbmax < 2) nbmax = 2;
+    nbmax += nbmax & 1;
+    const int rounds = nbmax - 1, pairs = nbmax / 2;
+    int npow2 = 1;
+    while (npow2 < lo.cslot) npow2 <<= 1;
+    const size_t sort_smem = (size_t)npow2 * (sizeof(float) + sizeof(int));
+    int host_counter[2] = {0, 0};   // pageable stack memory: no pinned buffer
+    int sweeps = 0;
+    bool converged = false;
+    if (cmax >= 2) {
+        for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
+            MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
+            if (cmax > 2 * bc) {
+                presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2);
+                MPS_LAUNCH_CHECK("presort_kernel");
+                gather_kernel<<<dim3(cmax, njobs), 128, 0, s>>>(jobs, g, X2, V2);
+                MPS_LAUNCH_CHECK("gather_kernel");
+                cf* t = g.X; g.X = X2; X2 = t;
+                t = g.V; g.V = V2; V2 = t;
+            }
+            for (int r = 0; r < rounds; ++r) {
+                rc = visit(jobs, njobs, pairs, g, r, tol, lw, s);
+                if (rc) return rc;
+            }
+            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol);
+            MPS_LAUNCH_CHECK("sweep_end_kernel");
+            MPS_CUDA_CHECK(cudaMemcpyAsync(host_counter, g.counter, sizeof(int),
+                                           cudaMemcpyDeviceToHost, s));
+            MPS_CUDA_CHECK(cudaStreamSynchronize(s));
+            if (host_counter[0] == 0) {
+                converged = true;
+                break;
+            }
+        }
+        if (sweeps > max_sweeps) sweeps = max_sweeps;
+    } else {
+        converged = true;
+        MPS_CUDA_CHECK(cudaMemsetAsync(g.done, 0xff, (size_t)njobs * sizeof(int), s));
+    }
+    if (params) params->sweeps_out = sweeps;
+
+    if (sort_smem > 48 * 1024) {
+        MPS_CUDA_CHECK(cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)sort_smem));
+    }
+    sort_kernel<<<njobs, SORT_T, sort_smem, s>>>(jobs, g, npow2);
+    MPS_LAUNCH_CHECK("sort_kernel");
+    {
+        const int kmax = cmax;
+        dim3 ga((kmax + 31) / 32, (max_m + 31) / 32, njobs);
+        regauge_a_kernel<<<ga, dim3(32, 8), 0, s>>>(jobs, g);
+        MPS_LAUNCH_CHECK("regauge_a_kernel");
+        dim3 gb((max_n + 255) / 256, kmax, njobs);
+        regauge_b_kernel<<<gb, 256, 0, s>>>(jobs, g);
+        MPS_LAUNCH_CHECK("regauge_b_kernel");
+        const size_t comp_smem = (size_t)(max(max_m, max_n) + kmax) * sizeof(cf);
+        if (comp_smem > 48 * 1024) {
+            MPS_CUDA_CHECK(cudaFuncSetAttribute(complete_kernel,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)comp_smem));
+        }
+        complete_kernel<<<njobs, COMP_T, comp_smem, s>>>(jobs, g);
+        MPS_LAUNCH_CHECK("complete_kernel");
+        dim3 gu((max_n + 63) / 64, (kmax + 63) / 64, njobs);
+        uh_theta_kernel<<<gu, 256, 0, s>>>(jobs, g);
+        MPS_LAUNCH_CHECK("uh_theta_kernel");
+    }
+    MPS_CUDA_CHECK(cudaMemcpyAsync(host_counter + 1, g.counter + 1, sizeof(int),
+                                   cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (host_counter[1] != 0)
+        return fail(MPS_ERR_NONFINITE, "mps_apply_2q_batch_noalloc: NaN/Inf singular value");
+    if (!converged)
+        return fail(MPS_ERR_NOT_CONVERGED, "mps_apply_2q_batch_noalloc: Jacobi SVD hit its sweep cap");
     return MPS_OK;
 }
