@@ -183,6 +183,57 @@ def run_reference(args, rank, world):
     return 0
 
 
+def run_batch_workload(args, rank, world):
+    """Multi-circuit workloads: batch_512_mixed and qutrit_128x32_d30_chi192.
+    A step is every circuit of the batch from |0...0> to its last layer."""
+    import torch
+    import __graft_entry__ as ge
+    from mpsim_gb300 import circuits as C
+    from mpsim_gb300 import _native
+    from mpsim_gb300.batch import run_circuits
+
+    ge.build()
+    torch.cuda.set_device(0)
+    if args.workload == "batch_512_mixed":
+        circs = C.mixed_batch(args.ncircuits or 512, seed=replica_instance(rank))
+    else:
+        circs = C.qutrit_batch(args.ncircuits or 128, seed=replica_instance(rank))
+    ngates = sum(c.n_two_qudit_gates for c in circs)
+    lib = _native.load()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        run_circuits(circs)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    l0 = lib.mps_kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        states = run_circuits(circs)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    line = {
+        "metric": f"two-qudit gates/s ({args.workload})", "value": ngates * args.steps / (ms / 1000.0),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded Haar gates)",
+        "config": {"workload": args.workload, "circuits": len(circs),
+                   "two_qudit_gates_per_step": ngates,
+                   "l2": "256 MiB buffer written at the start of every step"},
+        "circuits_per_s": len(circs) * args.steps / (ms / 1000.0),
+        "gpu_launches": int(lib.mps_kernel_launches() - l0), "clocks": clk,
+        "mean_norm": float(np.mean([s.norm() for s in states])),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -193,6 +244,7 @@ def main():
     ap.add_argument("--ref-gates", type=int, default=6)
     ap.add_argument("--cpu-gates", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncircuits", type=int, default=0)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -200,6 +252,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload in ("batch_512_mixed", "qutrit_128x32_d30_chi192"):
+        return run_batch_workload(args, rank, world)
 
     import torch
     import __graft_entry__ as ge

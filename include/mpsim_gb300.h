@@ -61,7 +61,7 @@ typedef struct {
 typedef struct {
     int32_t max_sweeps;    /* default 40                                   */
     float tol;             /* relative off-diagonal threshold; default
-                              2 * sqrt(rows) * 2^-24, at least 2^-22       */
+                              2^-24 * max(8, sqrt(rows))                   */
     int32_t block_cols;    /* columns per block: 8 or 16 (default 16)      */
     int32_t sweeps_out;    /* out: sweeps taken by the slowest job         */
 } mps_svd_params;
@@ -76,6 +76,19 @@ unsigned long long mps_kernel_launches(void);
  * Replaces MPS.apply_one_qudit_gate, unitary branch (mpsim/core.py:753-826). */
 int mps_apply_1q(void* stream, mps_c64* site, int chi_l, int d, int chi_r,
                  const mps_c64* gate);
+
+/* One-qudit gates on many sites (of one or many states) in one launch.
+ * 24 bytes; the Python side mirrors it field by field. */
+typedef struct {
+    mps_c64* site;         /* (chi_l, d, chi_r), updated in place           */
+    const mps_c64* gate;   /* (d, d) row-major U[a', a]                     */
+    int32_t chi_l, chi_r;
+} mps_1q_job;
+
+/* mps_apply_1q for njobs (site, gate) pairs in a device array; sites must not
+ * alias.  Same arithmetic as MPS.apply_one_qudit_gate, unitary branch
+ * (mpsim/core.py:820-826), batched over states for the multi-circuit form. */
+int mps_apply_1q_batch(void* stream, const mps_1q_job* jobs_dev, int njobs, int d);
 
 /* Workspace bytes mps_apply_2q_batch needs for njobs jobs whose merged
  * matrices are at most max_m x max_n (m = chi_l*d, n = d*chi_r). */

@@ -36,6 +36,11 @@ JOB_DTYPE = np.dtype([
 ])
 assert JOB_DTYPE.itemsize == 88
 
+# mps_1q_job (24 bytes).
+JOB1_DTYPE = np.dtype([("site", np.uint64), ("gate", np.uint64),
+                       ("chi_l", np.int32), ("chi_r", np.int32)])
+assert JOB1_DTYPE.itemsize == 24
+
 
 class SvdParams(ctypes.Structure):
     _fields_ = [("max_sweeps", ctypes.c_int32), ("tol", ctypes.c_float),
@@ -51,6 +56,7 @@ SIGNATURES = {
     "mps_last_error": (ctypes.c_char_p, []),
     "mps_kernel_launches": (ctypes.c_ulonglong, []),
     "mps_apply_1q": (_I, [_P, _P, _I, _I, _I, _P]),
+    "mps_apply_1q_batch": (_I, [_P, _P, _I, _I]),
     "mps_2q_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
     "mps_apply_2q_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _SZ, ctypes.POINTER(SvdParams)]),
     "mps_apply_2q_batch_noalloc": (_I, [_P, _P, _I, _I, _I, _I, ctypes.POINTER(SvdParams)]),

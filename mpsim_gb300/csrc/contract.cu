@@ -64,6 +64,38 @@ __global__ void apply_1q_kernel(cf* __restrict__ site, int chil, int d, int chir
     }
 }
 
+// Batched one-qudit gates: blockIdx.y selects the (site, gate) job.
+template <int DMAX>
+__global__ void apply_1q_batch_kernel(const mps_1q_job* __restrict__ jobs, int d) {
+    __shared__ cf U[DMAX * DMAX];
+    const mps_1q_job job = jobs[blockIdx.y];
+    const cf* gate = reinterpret_cast<const cf*>(job.gate);
+    for (int e = threadIdx.x; e < d * d; e += blockDim.x) U[e] = gate[e];
+    __syncthreads();
+    const int chil = job.chi_l, chir = job.chi_r;
+    const size_t total = (size_t)chil * chir;
+    cf* site = reinterpret_cast<cf*>(job.site);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const size_t l = t / chir, r = t % chir;
+        cf* base = site + l * d * chir + r;
+        cf v[DMAX];
+#pragma unroll
+        for (int a = 0; a < DMAX; ++a)
+            if (a < d) v[a] = base[(size_t)a * chir];
+#pragma unroll
+        for (int ap = 0; ap < DMAX; ++ap) {
+            if (ap < d) {
+                cf acc = cmake(0.f, 0.f);
+#pragma unroll
+                for (int a = 0; a < DMAX; ++a)
+                    if (a < d) cfma(acc, U[ap * d + a], v[a]);
+                base[(size_t)ap * chir] = acc;
+            }
+        }
+    }
+}
+
 __global__ void scale_kernel(cf* __restrict__ x, size_t count, cf alpha, int conj) {
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count;
          t += (size_t)gridDim.x * blockDim.x) {
@@ -214,6 +246,21 @@ extern "C" int mps_apply_1q(void* stream, mps_c64* site, int chi_l, int d, int c
     else if (d <= 16) apply_1q_kernel<16><<<blocks, 256, 0, s>>>(x, chi_l, d, chi_r, u);
     else apply_1q_kernel<64><<<blocks, 256, 0, s>>>(x, chi_l, d, chi_r, u);
     MPS_LAUNCH_CHECK("apply_1q_kernel");
+    return MPS_OK;
+}
+
+extern "C" int mps_apply_1q_batch(void* stream, const mps_1q_job* jobs, int njobs, int d) {
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (njobs == 0) return MPS_OK;
+    if (njobs < 0 || njobs > 65535 || !jobs) return fail(MPS_ERR_ARG, "mps_apply_1q_batch: bad job list");
+    if (d < 1 || d > 64) return fail(MPS_ERR_ARG, "mps_apply_1q_batch: bad qudit dimension");
+    dim3 grid(8, njobs);
+    if (d <= 2) apply_1q_batch_kernel<2><<<grid, 256, 0, s>>>(jobs, d);
+    else if (d <= 4) apply_1q_batch_kernel<4><<<grid, 256, 0, s>>>(jobs, d);
+    else if (d <= 8) apply_1q_batch_kernel<8><<<grid, 256, 0, s>>>(jobs, d);
+    else if (d <= 16) apply_1q_batch_kernel<16><<<grid, 256, 0, s>>>(jobs, d);
+    else apply_1q_batch_kernel<64><<<grid, 256, 0, s>>>(jobs, d);
+    MPS_LAUNCH_CHECK("apply_1q_batch_kernel");
     return MPS_OK;
 }
 

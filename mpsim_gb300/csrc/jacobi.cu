@@ -24,14 +24,15 @@
 // The tau form keeps c = 1 - s tau implicit: with an explicit c, tiny angles
 // round c up to exactly 1 and every such rotation grows the column norms; over
 // thousands of rotations that biases every singular value.  A pair is rotated
-// only when |gamma| > tol sqrt(alpha beta) (tol = 2 sqrt(L) 2^-24 by default);
+// only when |gamma| > tol sqrt(alpha beta) (tol = 2^-24 max(8, sqrt(L)) by
+// default);
 // a sweep with no rotation in a job marks the job converged.  Column norms
 // are recomputed from the rotated data, so they do not drift.
 //
 // V.  A job that is tall (m >= n) and left-canonical -- the default of
-// apply_two_qudit_gate -- needs only U = X_k / S: its right site S V^H equals
-// U^H theta, formed by one GEMM against a copy of theta, so such jobs never
-// accumulate V.  Other jobs accumulate the 2BC x 2BC rotation of each visit in
+// apply_two_qudit_gate -- needs only U = X_k / S: one Newton-Schulz step makes
+// U an isometry to rounding, and its right site S V^H equals U^H theta, one
+// GEMM against a copy of theta, so such jobs never accumulate V.  Other jobs accumulate the 2BC x 2BC rotation of each visit in
 // shared memory and apply V <- V Q.
 //
 // Afterwards sigma_c = |X_c|, sorted descending (ties by column index); the
@@ -50,7 +51,7 @@ namespace mps {
 namespace {
 
 struct Rot {
-    float s, tau;
+    float s, tau, t;
     cf e;
 };
 
@@ -61,6 +62,7 @@ __device__ __forceinline__ Rot make_rot(float a, float b, cf gam, float ag) {
                                : copysignf(1.f, zeta) / (az + sqrtf(fmaf(zeta, zeta, 1.f)));
     const float c = 1.f / sqrtf(fmaf(t, t, 1.f));
     Rot r;
+    r.t = t;
     r.s = c * t;
     r.tau = r.s / (1.f + c);
     r.e = cmake(gam.x / ag, -gam.y / ag);
@@ -234,6 +236,9 @@ full_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
 template <int BC, int ROWS>
 __global__ void __launch_bounds__(BC * 32)
 ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
+    // Every slot column has exactly 32*ROWS rows (lslot == 32*ROWS) and rows
+    // past the job's length are zero, so no row is predicated: zero rows stay
+    // zero under every rotation.
     extern __shared__ float2 smem[];
     const int j = blockIdx.y;
     if (g.done[j]) return;
@@ -242,11 +247,11 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
     if (round >= sh.nb - 1 || (int)blockIdx.x >= sh.nb / 2) return;
     int I, J;
     tournament_pair(sh.nb, round, blockIdx.x, I, J);
-    const int Lw = (sh.L + 31) & ~31;
+    constexpr int LW = 32 * ROWS;
     constexpr int W = 2 * BC;
     cf* X = g.X + (size_t)j * g.lslot * g.cslot;
-    cf* ring = smem;                            // [BC][Lw]
-    cf* Qs = smem + (size_t)BC * Lw;            // [W][W], column-major
+    cf* ring = smem;                            // [BC][LW]
+    cf* Qs = smem + (size_t)BC * LW;            // [W][W], column-major
     float* ringn = reinterpret_cast<float*>(Qs + W * W);  // [BC]
     __shared__ float s_off[BC];
 
@@ -258,9 +263,8 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
         const cf* vs = X + (size_t)(J * BC + warp) * g.lslot;
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
-            const int r = lane + 32 * i;
-            hx[i] = r < Lw ? hs[r] : cmake(0.f, 0.f);
-            vx[i] = r < Lw ? vs[r] : cmake(0.f, 0.f);
+            hx[i] = hs[lane + 32 * i];
+            vx[i] = vs[lane + 32 * i];
             hn += cabs2(hx[i]);
             vn += cabs2(vx[i]);
         }
@@ -286,15 +290,26 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
         offmax = fmaxf(offmax, rel);
         if (rel > tol) {
             const Rot R = make_rot(hn, vn, gam, ag);
-            float na = 0.f, nq = 0.f;
 #pragma unroll
-            for (int i = 0; i < ROWS; ++i) {
-                apply_rot(R, hx[i], vx[i]);
-                na += cabs2(hx[i]);
-                nq += cabs2(vx[i]);
+            for (int i = 0; i < ROWS; ++i) apply_rot(R, hx[i], vx[i]);
+            // closed-form norm update (Hestenes): |x'|^2 = |x|^2 - t|gamma|,
+            // |q'|^2 = |q|^2 + t|gamma|; recompute when cancellation leaves
+            // less than 1/16 of a norm (warp-uniform decision)
+            const float dn = R.t * ag;
+            float na = hn - dn, nq = vn + dn;
+            if (na < 0.0625f * hn || nq < 0.0625f * vn) {
+                na = 0.f;
+                nq = 0.f;
+#pragma unroll
+                for (int i = 0; i < ROWS; ++i) {
+                    na += cabs2(hx[i]);
+                    nq += cabs2(vx[i]);
+                }
+                na = warp_sum(na);
+                nq = warp_sum(nq);
             }
-            hn = warp_sum(na);
-            vn = warp_sum(nq);
+            hn = na;
+            vn = nq;
             if (sh.track_v && lane < W) {
                 cf qa = Qs[warp * W + lane], qb = Qs[(BC + vid) * W + lane];
                 apply_rot(R, qa, qb);
@@ -304,20 +319,14 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
         }
         if (step + 1 < BC) {
             const int to = (warp + 1) % BC;
-            cf* dst = ring + (size_t)to * Lw;
+            cf* dst = ring + (size_t)to * LW;
 #pragma unroll
-            for (int i = 0; i < ROWS; ++i) {
-                const int r = lane + 32 * i;
-                if (r < Lw) dst[r] = vx[i];
-            }
+            for (int i = 0; i < ROWS; ++i) dst[lane + 32 * i] = vx[i];
             if (lane == 0) ringn[to] = vn;
             __syncthreads();
-            const cf* src = ring + (size_t)warp * Lw;
+            const cf* src = ring + (size_t)warp * LW;
 #pragma unroll
-            for (int i = 0; i < ROWS; ++i) {
-                const int r = lane + 32 * i;
-                vx[i] = r < Lw ? src[r] : cmake(0.f, 0.f);
-            }
+            for (int i = 0; i < ROWS; ++i) vx[i] = src[lane + 32 * i];
             vn = ringn[warp];
             vid = (vid + BC - 1) % BC;
             __syncthreads();
@@ -328,11 +337,8 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
         cf* vd = X + (size_t)(J * BC + vid) * g.lslot;
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
-            const int r = lane + 32 * i;
-            if (r < Lw) {
-                hd[r] = hx[i];
-                vd[r] = vx[i];
-            }
+            hd[lane + 32 * i] = hx[i];
+            vd[lane + 32 * i] = vx[i];
         }
     }
     if (sh.track_v) {
@@ -603,40 +609,74 @@ __global__ void regauge_b_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g
         out[c] = cscale(cconj(col[c]), sc);
 }
 
-// b_out = a_out^H theta for tall left-canonical jobs (S V^H = U^H theta).
-// 64x64 output tiles, K (= m) in chunks of 16, 256 threads x 4x4 outputs.
+// Post-processing GEMMs for tall left-canonical jobs (the V-free path), all
+// 64x64 output tiles, K in chunks of 16, 256 threads x 4x4 outputs:
+//   POST_GRAM : G = U^H U          (k x k, into the job's V slot), U = a_out
+//   POST_APPLY: U' = U (3I - G)/2  (m x k, into the job's X slot): one
+//               Newton-Schulz step, which squares U's distance from an
+//               isometry (the Jacobi tolerance) so U U^H is a projector to
+//               rounding, as LAPACK's U would give
+//   POST_UH   : S V^H = U'^H theta (k x n, into b_out), theta = the T copy
+//   POST_COPY : a_out = U'
+enum PostMode { POST_GRAM = 0, POST_APPLY = 1, POST_UH = 2 };
+
+template <int MODE>
 __global__ void __launch_bounds__(256)
-uh_theta_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
+post_gemm_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
     __shared__ cf As[16][64];
     __shared__ cf Bs[16][64];
     const int j = blockIdx.z;
     const mps_2q_job job = jobs[j];
     const int m = job.chi_l * g.d, n = job.chi_r * g.d, k = job.k;
     if (job_tracks_v(m, n, job.keep_left_canonical)) return;
+    int M, N, K;
+    if (MODE == POST_GRAM) { M = k; N = k; K = m; }
+    else if (MODE == POST_APPLY) { M = m; N = k; K = k; }
+    else { M = k; N = n; K = m; }
     const int i0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
-    if (i0 >= k || c0 >= n) return;
-    const cf* U = reinterpret_cast<const cf*>(job.a_out);     // m x k row-major
-    const cf* T = g.T + (size_t)j * g.lslot * g.cslot;        // theta, column-major
+    if (i0 >= M || c0 >= N) return;
+    const cf* U = reinterpret_cast<const cf*>(job.a_out);          // m x k row-major
+    cf* Gm = g.V + (size_t)j * g.cslot * g.cslot;                   // k x k row-major
+    cf* Up = g.X + (size_t)j * g.lslot * g.cslot;                   // m x k row-major
+    const cf* T = g.T + (size_t)j * g.lslot * g.cslot;              // theta, column-major
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     cf acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) acc[a][b] = cmake(0.f, 0.f);
-    for (int r0 = 0; r0 < m; r0 += 16) {
+    for (int l0 = 0; l0 < K; l0 += 16) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int idx = tid + q * 256;
-            const int ti = idx & 63, kk = idx >> 6;
-            const int row = r0 + kk, i = i0 + ti;
-            As[kk][ti] = (row < m && i < k) ? cconj(U[(size_t)row * k + i]) : cmake(0.f, 0.f);
+            int ti, kk;
+            if (MODE == POST_APPLY) { kk = idx & 15; ti = idx >> 4; }   // U rows: l contiguous
+            else { ti = idx & 63; kk = idx >> 6; }                     // U^H: i contiguous
+            const int i = i0 + ti, l = l0 + kk;
+            cf v = cmake(0.f, 0.f);
+            if (i < M && l < K) {
+                if (MODE == POST_GRAM) v = cconj(U[(size_t)l * k + i]);
+                else if (MODE == POST_APPLY) v = U[(size_t)i * k + l];
+                else v = cconj(Up[(size_t)l * k + i]);
+            }
+            As[kk][ti] = v;
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int idx = tid + q * 256;
-            const int kk = idx & 15, tc = idx >> 4;
-            const int row = r0 + kk, c = c0 + tc;
-            Bs[kk][tc] = (row < m && c < n) ? T[(size_t)c * g.lslot + row] : cmake(0.f, 0.f);
+            int tc, kk;
+            if (MODE == POST_UH) { kk = idx & 15; tc = idx >> 4; }      // theta column-major
+            else { tc = idx & 63; kk = idx >> 6; }
+            const int c = c0 + tc, l = l0 + kk;
+            cf v = cmake(0.f, 0.f);
+            if (c < N && l < K) {
+                if (MODE == POST_GRAM) v = U[(size_t)l * k + c];
+                else if (MODE == POST_APPLY) {
+                    const cf gl = Gm[(size_t)l * k + c];
+                    v = cmake((l == c ? 1.5f : 0.f) - 0.5f * gl.x, -0.5f * gl.y);
+                } else v = T[(size_t)c * g.lslot + l];
+            }
+            Bs[kk][tc] = v;
         }
         __syncthreads();
 #pragma unroll
@@ -653,14 +693,47 @@ uh_theta_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
         }
         __syncthreads();
     }
-    cf* out = reinterpret_cast<cf*>(job.b_out);
+    cf* out;
+    size_t ld;
+    if (MODE == POST_GRAM) { out = Gm; ld = (size_t)k; }
+    else if (MODE == POST_APPLY) { out = Up; ld = (size_t)k; }
+    else { out = reinterpret_cast<cf*>(job.b_out); ld = (size_t)n; }
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             const int i = i0 + ty + 16 * a, c = c0 + tx + 16 * b;
-            if (i < k && c < n) out[(size_t)i * n + c] = acc[a][b];
+            if (i < M && c < N) out[(size_t)i * ld + c] = acc[a][b];
         }
+}
+
+// a_out = U' (the X slot) for tall left-canonical jobs.
+__global__ void post_copy_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
+    const int j = blockIdx.y;
+    const mps_2q_job job = jobs[j];
+    const int m = job.chi_l * g.d, n = job.chi_r * g.d;
+    if (job_tracks_v(m, n, job.keep_left_canonical)) return;
+    const size_t total = (size_t)m * job.k;
+    const cf* src = g.X + (size_t)j * g.lslot * g.cslot;
+    cf* dst = reinterpret_cast<cf*>(job.a_out);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x)
+        dst[e] = src[e];
+}
+
+int launch_post(const mps_2q_job* jobs, int njobs, int max_m, int max_n, int kmax,
+                const TwoQGeom& g, cudaStream_t s) {
+    post_gemm_kernel<POST_GRAM><<<dim3((kmax + 63) / 64, (kmax + 63) / 64, njobs), 256, 0, s>>>(jobs, g);
+    MPS_LAUNCH_CHECK("post_gemm_kernel<gram>");
+    post_gemm_kernel<POST_APPLY><<<dim3((kmax + 63) / 64, (max_m + 63) / 64, njobs), 256, 0, s>>>(jobs, g);
+    MPS_LAUNCH_CHECK("post_gemm_kernel<apply>");
+    post_gemm_kernel<POST_UH><<<dim3((max_n + 63) / 64, (kmax + 63) / 64, njobs), 256, 0, s>>>(jobs, g);
+    MPS_LAUNCH_CHECK("post_gemm_kernel<uh>");
+    const size_t total = (size_t)max_m * kmax;
+    int blocks = (int)((total + 255) / 256 < 1024 ? (total + 255) / 256 : 1024);
+    post_copy_kernel<<<dim3(blocks > 0 ? blocks : 1, njobs), 256, 0, s>>>(jobs, g);
+    MPS_LAUNCH_CHECK("post_copy_kernel");
+    return MPS_OK;
 }
 
 // Orthonormal completion of the isometric factor where sigma is an exact
@@ -826,10 +899,19 @@ struct Layout {
         off_counter, total;
 };
 
+// Column length of a slot: the ring kernel reads exactly 32*ROWS rows, so
+// the slot is padded up to the ROWS step pick_visit chooses for it.
+int slot_rows(int L) {
+    const int steps[] = {64, 128, 256, 512, 576, 1024, 1792};
+    for (int r : steps)
+        if (L <= r) return r;
+    return (int)align_up((size_t)L, 32);
+}
+
 Layout make_layout(int njobs, int max_m, int max_n) {
     Layout lo;
     const int L = max(max_m, max_n), C = min(max_m, max_n);
-    lo.lslot = (int)align_up((size_t)max(L, 1), 32);
+    lo.lslot = slot_rows(max(L, 1));
     lo.cslot = (int)align_up((size_t)max(C, 1), 32);
     size_t o = 0;
     const size_t nj = (size_t)max(njobs, 1);
@@ -901,11 +983,13 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         if (params->max_sweeps > 0) max_sweeps = params->max_sweeps;
         tol = params->tol;
     }
-    // The computed x_p^H x_q carries a rounding error of about sqrt(L) 2^-24
-    // |x_p||x_q|; a threshold at that floor keeps rotating noise.  Twice it
-    // leaves the factors orthonormal to a few 1e-6 and the singular values
-    // (second order in the residual) far more accurate.
-    if (!(tol > 0.f)) tol = fmaxf(2.f * sqrtf((float)lo.lslot) * 5.9604645e-8f, 2.3841858e-7f);
+    // The computed x_p^H x_q carries a rounding error of a few 2^-24
+    // sum_r |x_r||q_r|, growing slowly with the length L; the default
+    // threshold 2^-24 max(8, sqrt(L)) stays above that noise (no sweep keeps
+    // rotating noise) while the kept subspace -- whose error is about
+    // tol s_k / gap at the truncation cut -- stays close to what a
+    // backward-stable complex64 SVD gives.
+    if (!(tol > 0.f)) tol = 5.9604645e-8f * fmaxf(8.f, sqrtf((float)lo.lslot));
     const int lw = lo.lslot;
     int bc = 16;
     visit_fn visit = pick_visit(lw, &bc);
@@ -996,9 +1080,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         }
         complete_kernel<<<njobs, COMP_T, comp_smem, s>>>(jobs, g);
         MPS_LAUNCH_CHECK("complete_kernel");
-        dim3 gu((max_n + 63) / 64, (kmax + 63) / 64, njobs);
-        uh_theta_kernel<<<gu, 256, 0, s>>>(jobs, g);
-        MPS_LAUNCH_CHECK("uh_theta_kernel");
+        rc = launch_post(jobs, njobs, max_m, max_n, kmax, g, s);
+        if (rc) return rc;
     }
     MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 1, g.counter + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
     MPS_CUDA_CHECK(cudaStreamSynchronize(s));
@@ -1099,7 +1182,7 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
         if (params->max_sweeps > 0) max_sweeps = params->max_sweeps;
         tol = params->tol;
     }
-    if (!(tol > 0.f)) tol = fmaxf(2.f * sqrtf((float)lo.lslot) * 5.9604645e-8f, 2.3841858e-7f);
+    if (!(tol > 0.f)) tol = 5.9604645e-8f * fmaxf(8.f, sqrtf((float)lo.lslot));
     const int lw = lo.lslot;
     int bc = 16;
     visit_fn visit = pick_visit(lw, &bc);
@@ -1186,9 +1269,8 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
         }
         complete_kernel<<<njobs, COMP_T, comp_smem, s>>>(jobs, g);
         MPS_LAUNCH_CHECK("complete_kernel");
-        dim3 gu((max_n + 63) / 64, (kmax + 63) / 64, njobs);
-        uh_theta_kernel<<<gu, 256, 0, s>>>(jobs, g);
-        MPS_LAUNCH_CHECK("uh_theta_kernel");
+        rc = launch_post(jobs, njobs, max_m, max_n, kmax, g, s);
+        if (rc) return rc;
     }
     MPS_CUDA_CHECK(cudaMemcpyAsync(host_counter + 1, g.counter + 1, sizeof(int),
                                    cudaMemcpyDeviceToHost, s));

@@ -156,13 +156,16 @@ def test_job_struct_layout_matches_header(tmp_path):
     src = tmp_path / "layout.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "mpsim_gb300.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu\\n\", sizeof(mps_2q_job),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(mps_2q_job),"
         " offsetof(mps_2q_job, status), offsetof(mps_2q_job, chi_l), offsetof(mps_2q_job, k),"
-        " sizeof(mps_svd_params)); return 0;}\n")
+        " sizeof(mps_svd_params), sizeof(mps_1q_job), offsetof(mps_1q_job, chi_r));"
+        " return 0;}\n")
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
-    size, off_status, off_chil, off_k, psize = map(int, out)
+    size, off_status, off_chil, off_k, psize, size1, off_chir1 = map(int, out)
+    assert size1 == _native.JOB1_DTYPE.itemsize
+    assert off_chir1 == _native.JOB1_DTYPE.fields["chi_r"][1]
     dt = _native.JOB_DTYPE
     assert size == dt.itemsize
     assert off_status == dt.fields["status"][1]
