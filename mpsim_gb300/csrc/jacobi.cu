@@ -55,17 +55,21 @@ struct Rot {
     cf e;
 };
 
+// zeta and t set only the rotation angle, so fast divisions do; the unit
+// phase e and c (and tau, which fixes c = 1 - s tau) are kept correctly
+// rounded because their errors would make the rotation non-unitary.
 __device__ __forceinline__ Rot make_rot(float a, float b, cf gam, float ag) {
-    const float zeta = (b - a) / (2.f * ag);
+    const float zeta = __fdividef(b - a, 2.f * ag);
     const float az = fabsf(zeta);
-    const float t = az > 1e10f ? 0.5f / zeta
-                               : copysignf(1.f, zeta) / (az + sqrtf(fmaf(zeta, zeta, 1.f)));
-    const float c = 1.f / sqrtf(fmaf(t, t, 1.f));
+    const float t = az > 1e10f ? __fdividef(0.5f, zeta)
+                               : copysignf(__fdividef(1.f, az + sqrtf(fmaf(zeta, zeta, 1.f))), zeta);
+    const float c = __frsqrt_rn(fmaf(t, t, 1.f));
     Rot r;
     r.t = t;
     r.s = c * t;
     r.tau = r.s / (1.f + c);
-    r.e = cmake(gam.x / ag, -gam.y / ag);
+    const float inv = __frsqrt_rn(cabs2(gam));
+    r.e = cmake(gam.x * inv, -gam.y * inv);
     return r;
 }
 
@@ -250,9 +254,9 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
     constexpr int LW = 32 * ROWS;
     constexpr int W = 2 * BC;
     cf* X = g.X + (size_t)j * g.lslot * g.cslot;
-    cf* ring = smem;                            // [BC][LW]
-    cf* Qs = smem + (size_t)BC * LW;            // [W][W], column-major
-    float* ringn = reinterpret_cast<float*>(Qs + W * W);  // [BC]
+    cf* ring = smem;                            // [2][BC][LW], double-buffered
+    cf* Qs = smem + (size_t)2 * BC * LW;        // [W][W], column-major
+    float* ringn = reinterpret_cast<float*>(Qs + W * W);  // [2][BC]
     __shared__ float s_off[BC];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -318,18 +322,22 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
             }
         }
         if (step + 1 < BC) {
+            // Pass the visitor to warp+1 through buffer (step & 1).  One
+            // barrier per step suffices: a warp writes buffer b again only
+            // two steps later, after the next barrier, by which time every
+            // warp has read its slot of b.
+            const int buf = step & 1;
             const int to = (warp + 1) % BC;
-            cf* dst = ring + (size_t)to * LW;
+            cf* dst = ring + ((size_t)buf * BC + to) * LW;
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) dst[lane + 32 * i] = vx[i];
-            if (lane == 0) ringn[to] = vn;
+            if (lane == 0) ringn[buf * BC + to] = vn;
             __syncthreads();
-            const cf* src = ring + (size_t)warp * LW;
+            const cf* src = ring + ((size_t)buf * BC + warp) * LW;
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) vx[i] = src[lane + 32 * i];
-            vn = ringn[warp];
+            vn = ringn[buf * BC + warp];
             vid = (vid + BC - 1) % BC;
-            __syncthreads();
         }
     }
     {
@@ -849,7 +857,8 @@ size_t full_smem(int lw) {
 
 template <int BC>
 size_t ring_smem(int lw) {
-    return (size_t)BC * lw * sizeof(cf) + (size_t)4 * BC * BC * sizeof(cf) + (size_t)BC * sizeof(float);
+    return (size_t)2 * BC * lw * sizeof(cf) + (size_t)4 * BC * BC * sizeof(cf) +
+           (size_t)2 * BC * sizeof(float);
 }
 
 template <int BC, int ROWS>

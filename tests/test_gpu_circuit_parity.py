@@ -4,10 +4,13 @@ brickwork_10q_d10_full and brickwork_8qutrit_d8_chi12 are compared with the
 reference's own results (tests/golden, produced by running mpsim/core.py)
 gate by gate.  At 48 and 64 qubits the truncated dynamics amplifies rounding
 (the reference in complex64 ends 10% away from itself in complex128 at 48
-qubits), so there the checks are: exact kept counts and bond dimensions, the
-reference's singular values gate by gate while the two agree to rounding, the
-norm history, and a tolerance band that scales with the reference's own
-complex64-vs-complex128 spread.
+qubits), so there the checks are: exact kept counts and bond dimensions at
+every gate; singular values within 2e-5 of s_0 at every gate until the
+circuit starts to discard weight; afterwards, against the reference's own
+complex64-vs-complex128 spread at each gate (median ratio <= 20, every gate
+within 100x + 1e-4); and the final norm within 10x the reference's spread
+(at least 1e-3 relative).  Gate-level parity at full size, free of this
+amplification, is in test_gpu_svd_kernel.py.
 """
 import os
 
@@ -69,6 +72,25 @@ def test_small_circuits_match_reference(cuda, name):
     assert list(mps.bond_dimensions()) == list(z["ref_c128_bonds"])
 
 
+def _chaotic_checks(errs, spreads, pre, tag):
+    """errs/spreads: per-gate max |s - s_ref| / s_ref[0] of this run and of
+    the complex64 reference (oracle) against complex128.  Gates before
+    ``pre`` (norm still > 0.999, hardly any weight discarded yet) must match
+    tightly; afterwards the truncated dynamics amplifies rounding about x1.4
+    per layer for any complex64 SVD, so the later gates are compared with the
+    reference's own complex64 spread: median ratio <= 20 and every gate
+    within 100x the spread + 1e-4."""
+    errs, spreads = np.asarray(errs), np.asarray(spreads)
+    assert np.all(errs[:pre] <= 2e-5), (tag, int(np.argmax(errs[:pre])), float(errs[:pre].max()))
+    late_e, late_s = errs[pre:], spreads[pre:]
+    if late_e.size:
+        ratio = late_e / (late_s + 1e-6)
+        assert np.median(ratio) <= 20.0, (tag, float(np.median(ratio)))
+        worst = int(np.argmax(late_e - 100 * late_s))
+        assert np.all(late_e <= 100 * late_s + 1e-4), (tag, pre + worst, float(late_e[worst]),
+                                                        float(late_s[worst]))
+
+
 def test_48q_chi128_against_reference(cuda):
     z = np.load(os.path.join(GOLDEN, "brickwork_48q_d24_chi128.npz"))
     circ = C.workload("brickwork_48q_d24_chi128")
@@ -76,14 +98,15 @@ def test_48q_chi128_against_reference(cuda):
     ref = spectra(z, "ref_c128")
     r64 = spectra(z, "ref_c64")
     assert list(mps.bond_dimensions()) == list(z["ref_c128_bonds"])
+    errs, spreads = [], []
     for g, (s, k, _) in enumerate(mps.svals_history):
         assert k == z["ref_c128_kept"][g]
-        # the reference's own complex64 spread at this gate sets the band
-        spread = np.max(np.abs(r64[g][:k] - ref[g][:k])) / ref[g][0]
-        err = np.max(np.abs(s[:k] - ref[g][:k])) / ref[g][0]
-        assert err <= 20 * spread + 2e-5, (g, err, spread)
-    n_ref = z["ref_c128_norms"][-1]
-    assert abs(mps.norm() - n_ref) / n_ref < 5e-3
+        errs.append(np.max(np.abs(s[:k] - ref[g][:k])) / ref[g][0])
+        spreads.append(np.max(np.abs(r64[g][:k] - ref[g][:k])) / ref[g][0])
+    pre = int(np.searchsorted(-z["ref_c128_norms"], -0.999))
+    _chaotic_checks(errs, spreads, pre, "48q")
+    n_ref, n64 = z["ref_c128_norms"][-1], z["ref_c64_norms"][-1]
+    assert abs(mps.norm() - n_ref) / n_ref < max(10 * abs(n64 - n_ref) / n_ref, 1e-3)
 
 
 def test_64q_chi256_against_oracle(cuda):
@@ -94,16 +117,19 @@ def test_64q_chi256_against_oracle(cuda):
     off = z["oracle_c128_offsets"]
     head = z["oracle_c128_svals_head"]
     h64 = z["oracle_c64_svals_head"]
+    disc = z["oracle_c128_discarded"]
     assert list(mps.bond_dimensions()) == list(z["oracle_c128_bonds"])
-    for g, (s, k, disc) in enumerate(mps.svals_history):
+    errs, spreads = [], []
+    for g, (s, k, _) in enumerate(mps.svals_history):
         assert k == z["oracle_c128_kept"][g]
         ref = head[off[g]:off[g + 1]].astype(np.float64)
         r64 = h64[off[g]:off[g + 1]].astype(np.float64)
         h = len(ref)
-        spread = np.max(np.abs(r64 - ref)) / ref[0]
-        err = np.max(np.abs(s[:h] - ref)) / ref[0]
-        assert err <= 20 * spread + 2e-5, (g, err, spread)
+        errs.append(np.max(np.abs(s[:h] - ref)) / ref[0])
+        spreads.append(np.max(np.abs(r64 - ref)) / ref[0])
+    # gates before the first one that discards more than 1e-3 of its weight
+    pre = int(np.argmax(disc > 1e-3)) if np.any(disc > 1e-3) else len(disc)
+    _chaotic_checks(errs, spreads, pre, "64q")
     n_ref = float(z["oracle_c128_norm"])
     n64 = float(z["oracle_c64_norm"])
-    band = max(10 * abs(n64 - n_ref) / n_ref, 1e-3)
-    assert abs(mps.norm() - n_ref) / n_ref < band
+    assert abs(mps.norm() - n_ref) / n_ref < max(10 * abs(n64 - n_ref) / n_ref, 1e-3)
