@@ -15,7 +15,8 @@ both sides and the slowest rank's time counts.
 
 ``--impl reference`` times the reference's CPU algorithm (the NumPy oracle
 port: the same merge, LAPACK SVD and regauge per gate) on the host cores, on
-a bounded sample of the same workload: gates at chi=256 (theta 512x512).
+a bounded sample of the same workload: one gate of every distinct gate shape
+of the circuit, weighted by how often the shape occurs.
 """
 
 from __future__ import annotations
@@ -119,61 +120,111 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(ngates=6, chi=256, d=2, seed=123):
-    """Oracle port on steady-state gates: random chi=256 sites, Haar gate,
-    maxsvals=256 (merge, np.linalg.svd, regauge).  Returns (gates/s, seconds,
-    seconds of one per-gate norm sweep at 64 sites)."""
+def circuit_shapes(circ):
+    """Counts of (chi_l, chi_m, chi_r) over the circuit's two-qudit gates and of
+    (chi_l, chi_r) over its one-qudit gates.  Bond dimensions are fixed by the
+    circuit (kept count = min(maxsvals, min(chi_l d, d chi_r))), so no
+    simulation is needed."""
+    from collections import Counter
+    from mpsim_gb300.core import kept_count
+    n, d = circ.nqudits, circ.d
+    bonds = [1] * (n + 1)
+    two, one = Counter(), Counter()
+    for lay in circ.layers:
+        for i in range(n):
+            one[(bonds[i], bonds[i + 1])] += 1
+        for i in lay.pair_left:
+            i = int(i)
+            cl, cm, cr = bonds[i], bonds[i + 1], bonds[i + 2]
+            two[(cl, cm, cr)] += 1
+            bonds[i + 1] = kept_count(circ.maxsvals, min(cl * d, d * cr))
+    return one, two
+
+
+def _time_call(fn, min_seconds=0.02):
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        fn()
+        reps += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            return dt / reps
+
+
+def cpu_sample(circ, seed=123):
+    """The reference's CPU algorithm (NumPy oracle port: merge, LAPACK SVD,
+    regauge; one-qudit contraction) timed on one gate of every distinct shape
+    of ``circ``, weighted by how often each shape occurs.  Returns (two-qudit
+    gates/s over the whole circuit, seconds spent timing, per-gate seconds of
+    the per-gate norm sweep the reference also runs, at the largest bond)."""
     from oracle.ref_mps import OracleMPS
     from mpsim_gb300.circuits import haar_random_matrix
     rng = np.random.default_rng(seed)
-    o = OracleMPS(4, d, np.complex64)
-    sites = []
-    for shape in [(1, d, chi), (chi, d, chi), (chi, d, chi), (chi, d, 1)]:
+    d = circ.d
+    one, two = circuit_shapes(circ)
+    t_start = time.perf_counter()
+
+    def rnd(shape):
         t = (rng.normal(size=shape) + 1j * rng.normal(size=shape)).astype(np.complex64)
-        sites.append(t / np.sqrt(t.size))
-    o.sites = sites
-    t0 = time.perf_counter()
-    for q in range(ngates):
-        g = haar_random_matrix(2, d, 1000 + q)
-        o.sites[1] = sites[1]
-        o.sites[2] = sites[2]
-        o.apply_two_qudit_gate(g, 1, 2, maxsvals=chi)
-    dt = time.perf_counter() - t0
-    # one transfer step of the reference's per-gate norm sweep, times 64 sites
-    a = sites[1]
-    t1 = time.perf_counter()
-    env = np.eye(chi, dtype=np.complex64)
-    t = np.tensordot(env, np.conj(a), axes=([1], [0]))
-    env = np.tensordot(a, t, axes=([0, 1], [0, 1]))
-    norm_step = time.perf_counter() - t1
-    return ngates / dt, dt, norm_step * 64
+        return t / np.sqrt(t.size)
+
+    total = 0.0
+    g2 = haar_random_matrix(2, d, 1000)
+    for (cl, cm, cr), count in two.items():
+        a, b = rnd((cl, d, cm)), rnd((cm, d, cr))
+        o = OracleMPS(2, d, np.complex64)
+
+        def gate():
+            o.sites = [a, b]
+            o.apply_two_qudit_gate(g2, 0, 1, maxsvals=circ.maxsvals)
+        total += count * _time_call(gate)
+    g1 = haar_random_matrix(1, d, 1001)
+    for (cl, cr), count in one.items():
+        o = OracleMPS(2, d, np.complex64)
+        s = rnd((cl, d, cr))
+
+        def gate1():
+            o.sites[0] = s
+            o.apply_one_qudit_gate(g1, 0)
+        total += count * _time_call(gate1, 0.005)
+    chi = max(c[1] for c in two)
+    a = rnd((chi, d, chi))
+
+    def norm_step():
+        env = np.eye(chi, dtype=np.complex64)
+        t = np.tensordot(env, np.conj(a), axes=([1], [0]))
+        np.tensordot(a, t, axes=([0, 1], [0, 1]))
+    norm_per_gate = circ.nqudits * _time_call(norm_step)
+    ngates = sum(two.values())
+    return ngates / total, time.perf_counter() - t_start, norm_per_gate, len(two), len(one)
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
+    from mpsim_gb300 import circuits as C
+    circ = C.workload(args.workload if args.workload in C.WORKLOADS else WORKLOAD)
     for _ in range(args.warmup):
-        cpu_sample(ngates=2)
-    per = []
+        cpu_sample(circ)
+    rates = []
     t_all = time.perf_counter()
-    gates = 0
-    norm_cost = None
     for _ in range(args.steps):
-        rate, dt, norm_cost = cpu_sample(ngates=args.ref_gates)
-        per.append(dt)
-        gates += args.ref_gates
+        rate, spent, norm_cost, n2, n1 = cpu_sample(circ)
+        rates.append(rate)
     total = time.perf_counter() - t_all
-    value = gates / sum(per)
+    value = float(np.mean(rates))
     cores = os.cpu_count()
-    sample = (f"{args.ref_gates} steady-state chi=256 gates per step (theta 512x512 complex64, "
-              f"np.linalg.svd via the NumPy oracle port of mpsim/core.py:1059-1145; no per-gate "
-              f"norm sweep -- the reference as shipped adds one, ~{norm_cost:.3f}s per gate at 64 sites)")
+    sample = (f"NumPy oracle port of mpsim/core.py (merge, np.linalg.svd, regauge; one-qudit "
+              f"contraction) timed on one gate of each of the {n2} two-qudit and {n1} one-qudit "
+              f"shapes of the {circ.nqudits}-qubit depth-{circ.depth} circuit and weighted by their "
+              f"counts, {cores} host threads; excludes the per-gate norm sweep the reference runs "
+              f"after every two-qudit gate (~{norm_cost:.3f}s per gate at chi=256)")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
-        "data": "synthetic (seeded Haar gates, random chi=256 sites)",
-        "config": {"workload": WORKLOAD, "sample": "steady-state chi=256 gates"},
+        "data": "synthetic (seeded Haar gates, random sites of each gate shape)",
+        "config": {"workload": circ_name(circ), "sample": "shape-weighted gate sample"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
@@ -181,6 +232,10 @@ def run_reference(args, rank, world):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def circ_name(circ):
+    return f"brickwork_{circ.nqudits}q_d{circ.depth}_chi{circ.maxsvals}"
 
 
 def run_batch_workload(args, rank, world):
@@ -241,8 +296,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
-    ap.add_argument("--ref-gates", type=int, default=6)
-    ap.add_argument("--cpu-gates", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncircuits", type=int, default=0)
     args = ap.parse_args()
@@ -363,11 +416,12 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rate, dt, norm_cost = cpu_sample(ngates=args.cpu_gates)
+        rate, dt, norm_cost, n2, n1 = cpu_sample(circ)
         cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{args.cpu_gates} steady-state chi=256 gates (theta 512x512) through the "
-                         f"NumPy oracle port, {dt:.1f}s; per-gate norm sweep of the reference "
-                         f"as shipped not included (~{norm_cost:.3f}s per gate)"}
+               "sample": f"NumPy oracle port on one gate of each of the {n2} two-qudit and {n1} "
+                         f"one-qudit shapes of this circuit, weighted by their counts ({dt:.1f}s "
+                         f"of timing); excludes the reference's per-gate norm sweep "
+                         f"(~{norm_cost:.3f}s per gate at chi=256)"}
 
     if rank == 0:
         line = {
