@@ -33,6 +33,7 @@ extern "C" {
 #define MPS_ERR_WORKSPACE 3    /* workspace too small                       */
 #define MPS_ERR_NOT_CONVERGED 4/* Jacobi SVD hit its sweep cap              */
 #define MPS_ERR_NONFINITE 5    /* NaN/Inf met in a singular value           */
+#define MPS_ERR_TIMEOUT 6      /* a bounded in-kernel wait expired          */
 
 /* Per-job status bits written by mps_apply_2q_batch. */
 #define MPS_STATUS_NOT_CONVERGED 1
@@ -62,8 +63,14 @@ typedef struct {
     int32_t max_sweeps;    /* default 40                                   */
     float tol;             /* relative off-diagonal threshold; default
                               2^-24 * max(8, sqrt(rows))                   */
-    int32_t block_cols;    /* columns per block: 8 or 16 (default 16)      */
+    int32_t block_cols;    /* out: columns per block the kernel used       */
     int32_t sweeps_out;    /* out: sweeps taken by the slowest job         */
+    int32_t wait_limit;    /* max polls of a round-dependency wait inside a
+                              sweep (default 1<<22, ~0.3 s); on expiry the
+                              call returns MPS_ERR_TIMEOUT                 */
+    int32_t stall_test;    /* test hook: nonzero makes one wait target a
+                              round that never completes, so the wait must
+                              expire (with a small wait_limit)             */
 } mps_svd_params;
 
 /* Library version and build description. */

@@ -21,6 +21,7 @@ MPS_ERR_CUDA = 2
 MPS_ERR_WORKSPACE = 3
 MPS_ERR_NOT_CONVERGED = 4
 MPS_ERR_NONFINITE = 5
+MPS_ERR_TIMEOUT = 6
 NOALLOC_SCRATCH_BYTES = 32 << 20       # MPS_NOALLOC_SCRATCH_BYTES
 
 STATUS_NOT_CONVERGED = 1
@@ -44,7 +45,8 @@ assert JOB1_DTYPE.itemsize == 24
 
 class SvdParams(ctypes.Structure):
     _fields_ = [("max_sweeps", ctypes.c_int32), ("tol", ctypes.c_float),
-                ("block_cols", ctypes.c_int32), ("sweeps_out", ctypes.c_int32)]
+                ("block_cols", ctypes.c_int32), ("sweeps_out", ctypes.c_int32),
+                ("wait_limit", ctypes.c_int32), ("stall_test", ctypes.c_int32)]
 
 
 # (name, restype, argtypes) for every symbol the header declares.

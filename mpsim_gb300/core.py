@@ -808,8 +808,8 @@ class MPS:
         new._sites = [t.clone() for t in self._sites]
         new._norms = list(self._norms)
         new.svals_history = list(self.svals_history)
-        new.svd_params = _native.SvdParams(self.svd_params.max_sweeps, self.svd_params.tol,
-                                           self.svd_params.block_cols, 0)
+        new.svd_params = _native.SvdParams(self.svd_params.max_sweeps, self.svd_params.tol, 0, 0,
+                                           self.svd_params.wait_limit, 0)
         return new
 
     def __str__(self):

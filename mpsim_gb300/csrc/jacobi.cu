@@ -112,7 +112,7 @@ __device__ __forceinline__ void update_v(cf* V, int cslot, int C, int I, int J, 
     for (int r = threadIdx.x; r < C; r += BC * 32) {
         cf v[W];
 #pragma unroll
-        for (int c = 0; c < W; ++c) v[c] = V[(size_t)block_col(c, I, J, BC) * cslot + r];
+        for (int c = 0; c < W; ++c) v[c] = __ldcg(V + (size_t)block_col(c, I, J, BC) * cslot + r);
 #pragma unroll 4
         for (int c2 = 0; c2 < W; ++c2) {
             cf acc = cmake(0.f, 0.f);
@@ -138,29 +138,30 @@ __device__ __forceinline__ void publish_offmax(float offmax, float* s_off, int n
 // ---------------------------------------------------------------------------
 // Round 0: all pairs among the 2*BC staged columns.  ROWS = rows per lane
 // held in registers (working column length Lw <= 32*ROWS).
+// Loads of X and V use __ldcg (L2, bypassing L1): inside the persistent
+// sweep kernel another CTA may have rewritten a column since this SM last
+// cached it.
 template <int BC, int ROWS>
-__global__ void __launch_bounds__(BC * 32)
-full_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
-    extern __shared__ float2 smem[];
-    const int j = blockIdx.y;
+__device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, const TwoQGeom& g,
+                                           int j, int round, int pair, float tol, float2* smem,
+                                           float* s_off) {
     if (g.done[j]) return;
     const JobShape sh = job_shape<BC>(jobs, j, g.d);
     if (sh.C < 2) return;
-    if (round >= sh.nb - 1 || (int)blockIdx.x >= sh.nb / 2) return;
+    if (round >= sh.nb - 1 || pair >= sh.nb / 2) return;
     int I, J;
-    tournament_pair(sh.nb, round, blockIdx.x, I, J);
+    tournament_pair(sh.nb, round, pair, I, J);
     const int Lw = (sh.L + 31) & ~31;
     constexpr int W = 2 * BC;
     cf* X = g.X + (size_t)j * g.lslot * g.cslot;
     cf* Xs = smem;                              // [W][Lw]
     cf* Qs = smem + (size_t)W * Lw;             // [W][W], column-major
     float* nrm = reinterpret_cast<float*>(Qs + W * W);   // [W]
-    __shared__ float s_off[BC];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int c = warp; c < W; c += BC) {
         const cf* src = X + (size_t)block_col(c, I, J, BC) * g.lslot;
-        for (int r = lane; r < Lw; r += 32) Xs[(size_t)c * Lw + r] = src[r];
+        for (int r = lane; r < Lw; r += 32) Xs[(size_t)c * Lw + r] = __ldcg(src + r);
     }
     if (sh.track_v)
         for (int e = tid; e < W * W; e += BC * 32)
@@ -234,30 +235,36 @@ full_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
     publish_offmax(offmax, s_off, BC, g.offmax + j);
 }
 
+template <int BC, int ROWS>
+__global__ void __launch_bounds__(BC * 32)
+full_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
+    extern __shared__ float2 smem[];
+    __shared__ float s_off[BC];
+    visit_full<BC, ROWS>(jobs, g, blockIdx.y, round, blockIdx.x, tol, smem, s_off);
+}
+
 // ---------------------------------------------------------------------------
 // Rounds >= 1: the BC*BC pairs between block I (home, warp w holds column
 // I*BC+w) and block J (visitors, passed to warp w+1 after every step).
 template <int BC, int ROWS>
-__global__ void __launch_bounds__(BC * 32)
-ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
+__device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, const TwoQGeom& g,
+                                           int j, int round, int pair, float tol, float2* smem,
+                                           float* s_off) {
     // Every slot column has exactly 32*ROWS rows (lslot == 32*ROWS) and rows
     // past the job's length are zero, so no row is predicated: zero rows stay
     // zero under every rotation.
-    extern __shared__ float2 smem[];
-    const int j = blockIdx.y;
     if (g.done[j]) return;
     const JobShape sh = job_shape<BC>(jobs, j, g.d);
     if (sh.C < 2) return;
-    if (round >= sh.nb - 1 || (int)blockIdx.x >= sh.nb / 2) return;
+    if (round >= sh.nb - 1 || pair >= sh.nb / 2) return;
     int I, J;
-    tournament_pair(sh.nb, round, blockIdx.x, I, J);
+    tournament_pair(sh.nb, round, pair, I, J);
     constexpr int LW = 32 * ROWS;
     constexpr int W = 2 * BC;
     cf* X = g.X + (size_t)j * g.lslot * g.cslot;
     cf* ring = smem;                            // [2][BC][LW], double-buffered
     cf* Qs = smem + (size_t)2 * BC * LW;        // [W][W], column-major
     float* ringn = reinterpret_cast<float*>(Qs + W * W);  // [2][BC]
-    __shared__ float s_off[BC];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     cf hx[ROWS], vx[ROWS];
@@ -267,8 +274,8 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
         const cf* vs = X + (size_t)(J * BC + warp) * g.lslot;
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
-            hx[i] = hs[lane + 32 * i];
-            vx[i] = vs[lane + 32 * i];
+            hx[i] = __ldcg(hs + lane + 32 * i);
+            vx[i] = __ldcg(vs + lane + 32 * i);
             hn += cabs2(hx[i]);
             vn += cabs2(vx[i]);
         }
@@ -354,6 +361,84 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
         update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
     }
     publish_offmax(offmax, s_off, BC, g.offmax + j);
+}
+
+template <int BC, int ROWS>
+__global__ void __launch_bounds__(BC * 32)
+ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
+    extern __shared__ float2 smem[];
+    __shared__ float s_off[BC];
+    visit_ring<BC, ROWS>(jobs, g, blockIdx.y, round, blockIdx.x, tol, smem, s_off);
+}
+
+// ---------------------------------------------------------------------------
+// One whole sweep in one launch.  Persistent CTAs take items (round, job,
+// block pair) in round-major order from an atomic counter; an item of round
+// r > 0 first waits until both of its blocks have finished round r-1.  All
+// items of round r-1 are handed out before any item of round r and a CTA
+// holds one item at a time, so every awaited item is held by a running CTA:
+// no deadlock, whatever number of CTAs is resident.  The wait polls a flag
+// at most wait_limit times (with __nanosleep backoff); on expiry it raises
+// the error flag and the CTA leaves, as do the others once they see it.
+template <int BC, int ROWS>
+__global__ void __launch_bounds__(BC * 32)
+sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol, int njobs, int rounds,
+             int pairs, SweepSync sync) {
+    extern __shared__ float2 smem[];
+    __shared__ float s_off[BC];
+    __shared__ int s_item, s_abort;
+    const int per_round = njobs * pairs;
+    const int total = rounds * per_round;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_item = atomicAdd(sync.next_item, 1);
+            s_abort = *reinterpret_cast<volatile int*>(sync.error);
+        }
+        __syncthreads();
+        const int item = s_item;
+        if (item >= total || s_abort) return;
+        const int r = item / per_round, rem = item - r * per_round;
+        const int j = rem / pairs, p = rem - (rem / pairs) * pairs;
+        bool active = !g.done[j];
+        int I = 0, J = 0, nb = 2;
+        if (active) {
+            const JobShape sh = job_shape<BC>(jobs, j, g.d);
+            nb = sh.nb;
+            active = sh.C >= 2 && r < sh.nb - 1 && p < sh.nb / 2;
+            if (active) tournament_pair(sh.nb, r, p, I, J);
+        }
+        if (active && r > 0) {
+            if (threadIdx.x == 0) {
+                volatile int* fl = sync.block_round + (size_t)j * sync.nbmax;
+                volatile int* err = sync.error;
+                // the test hook waits for a round no block ever reaches
+                const int need = (sync.stall_test && item == per_round) ? rounds + 1 : r - 1;
+                int polls = 0;
+                while ((fl[I] < need || fl[J] < need) && *err == 0) {
+                    if (++polls > sync.wait_limit) {
+                        atomicExch(sync.error, 1);
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+                s_abort = *err;
+                __threadfence();
+            }
+            __syncthreads();
+            if (s_abort) return;
+        }
+        if (active) {
+            if (r == 0) visit_full<BC, ROWS>(jobs, g, j, r, p, tol, smem, s_off);
+            else visit_ring<BC, ROWS>(jobs, g, j, r, p, tol, smem, s_off);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();
+                atomicExch(sync.block_round + (size_t)j * sync.nbmax + I, r);
+                atomicExch(sync.block_round + (size_t)j * sync.nbmax + J, r);
+            }
+        }
+        __syncthreads();
+    }
 }
 
 __global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol) {
@@ -885,6 +970,45 @@ int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g
     return MPS_OK;
 }
 
+template <int BC, int ROWS>
+int launch_sweep(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const TwoQGeom& g,
+                 float tol, int lw, const SweepSync& sync, cudaStream_t s) {
+    static std::once_flag once;
+    static int limit = 0, rc = MPS_OK, ctas = 0;
+    if (prepare_kernel(sweep_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
+    const size_t smem = ring_smem<BC>(lw);
+    if (smem > (size_t)limit) return fail(MPS_ERR_ARG, "jacobi: merged matrix too long for shared memory");
+    if (ctas == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        MPS_CUDA_CHECK(cudaGetDevice(&dev));
+        MPS_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        MPS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<BC, ROWS>,
+                                                                    BC * 32, smem));
+        ctas = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    const int items = rounds * njobs * pairs;
+    const int grid = items < ctas ? items : ctas;
+    if (grid <= 0) return MPS_OK;
+    sweep_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, tol, njobs, rounds, pairs, sync);
+    MPS_LAUNCH_CHECK("sweep_kernel");
+    return MPS_OK;
+}
+
+typedef int (*sweep_fn)(const mps_2q_job*, int, int, int, const TwoQGeom&, float, int,
+                        const SweepSync&, cudaStream_t);
+
+sweep_fn pick_sweep(int lw) {
+    if (lw <= 576) {
+        if (lw <= 64) return launch_sweep<16, 2>;
+        if (lw <= 128) return launch_sweep<16, 4>;
+        if (lw <= 256) return launch_sweep<16, 8>;
+        if (lw <= 512) return launch_sweep<16, 16>;
+        return launch_sweep<16, 18>;
+    }
+    if (lw <= 1024) return launch_sweep<8, 32>;
+    return launch_sweep<8, 56>;
+}
+
 typedef int (*visit_fn)(const mps_2q_job*, int, int, const TwoQGeom&, int, float, int, cudaStream_t);
 
 // Block width and register rows for a working column length lw (<= 1792).
@@ -905,7 +1029,8 @@ visit_fn pick_visit(int lw, int* bc) {
 struct Layout {
     int lslot, cslot;
     size_t off_X, off_X2, off_V, off_V2, off_T, off_sig, off_perm, off_off, off_done, off_need,
-        off_counter, total;
+        off_counter, off_sync, total;
+    int nbmax;
 };
 
 // Column length of a slot: the ring kernel reads exactly 32*ROWS rows, so
@@ -935,6 +1060,10 @@ Layout make_layout(int njobs, int max_m, int max_n) {
     lo.off_done = o; o = align_up(o + nj * sizeof(int), 256);
     lo.off_need = o; o = align_up(o + nj * sizeof(int), 256);
     lo.off_counter = o; o = align_up(o + 4 * sizeof(int), 256);
+    // sweep sync: next_item, error, then block_round[njobs][nbmax] (nbmax
+    // for the smallest block width, 8 columns)
+    lo.nbmax = (int)align_up((size_t)(lo.cslot + 7) / 8, 2);
+    lo.off_sync = o; o = align_up(o + (2 + nj * lo.nbmax) * sizeof(int), 256);
     lo.total = o;
     return lo;
 }
@@ -1001,8 +1130,16 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (!(tol > 0.f)) tol = 5.9604645e-8f * fmaxf(8.f, sqrtf((float)lo.lslot));
     const int lw = lo.lslot;
     int bc = 16;
-    visit_fn visit = pick_visit(lw, &bc);
+    (void)pick_visit(lw, &bc);
+    sweep_fn sweep = pick_sweep(lw);
     if (params) params->block_cols = bc;
+    SweepSync sync;
+    sync.next_item = reinterpret_cast<int*>(ws + lo.off_sync);
+    sync.error = sync.next_item + 1;
+    sync.block_round = sync.next_item + 2;
+    sync.nbmax = lo.nbmax;
+    sync.wait_limit = (params && params->wait_limit > 0) ? params->wait_limit : (1 << 22);
+    sync.stall_test = params ? params->stall_test : 0;
 
     cf* X2 = reinterpret_cast<cf*>(ws + lo.off_X2);
     cf* V2 = reinterpret_cast<cf*>(ws + lo.off_V2);
@@ -1045,15 +1182,22 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
                 cf* t = g.X; g.X = X2; X2 = t;
                 t = g.V; g.V = V2; V2 = t;
             }
-            for (int r = 0; r < rounds; ++r) {
-                rc = visit(jobs, njobs, pairs, g, r, tol, lw, s);
-                if (rc) return rc;
-            }
+            // one persistent launch runs every round of the sweep
+            MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, 2 * sizeof(int), s));
+            MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
+                                           (size_t)njobs * lo.nbmax * sizeof(int), s));
+            rc = sweep(jobs, njobs, rounds, pairs, g, tol, lw, sync, s);
+            if (rc) return rc;
             sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
             MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
+            MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 2, sync.error, sizeof(int),
+                                           cudaMemcpyDeviceToHost, s));
             MPS_CUDA_CHECK(cudaStreamSynchronize(s));
+            if (t_pinned[2] != 0)
+                return fail(MPS_ERR_TIMEOUT, "mps_apply_2q_batch: a round-dependency wait inside the "
+                                             "sweep kernel expired; results are invalid");
             if (t_pinned[0] == 0) {
                 converged = true;
                 break;

@@ -30,6 +30,16 @@ struct TwoQGeom {
     int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf
 };
 
+// Work distribution of the persistent sweep kernel.
+struct SweepSync {
+    int* next_item;   // atomic item counter (reset to 0 before each sweep)
+    int* error;       // set to 1 when a dependency wait expires
+    int* block_round; // [njobs][nbmax]: last round each block finished (-1)
+    int nbmax;
+    int wait_limit;
+    int stall_test;
+};
+
 // A job tracks the right rotations V unless it is tall (m >= n) and left-
 // canonical: then U = X/S is all the Jacobi iteration must produce, and the
 // right site S V^H = U^H theta comes from one GEMM against a copy of theta.

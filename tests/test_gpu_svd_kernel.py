@@ -191,3 +191,19 @@ def test_sweep_cap_reports(built_lib, cuda):
     assert rc == _native.MPS_ERR_NOT_CONVERGED
     assert res[0]["status"] & _native.STATUS_NOT_CONVERGED
     assert p.sweeps_out == 1
+
+
+def test_wait_timeout_reports_and_recovers(built_lib, cuda):
+    """The sweep kernel's round-dependency waits are bounded: the stall test
+    hook makes one wait target a round that never completes; with a small
+    wait limit the call must return MPS_ERR_TIMEOUT (no hang, no fault), and
+    the next call on the same context must work."""
+    rng = np.random.default_rng(12)
+    a, b, g = make_job_inputs(rng, 64, 64, 64, 2)          # 128 columns: 7 rounds per sweep
+    p = _native.SvdParams(0, 0.0, 0, 0, 2000, 1)
+    rc, _, _ = run_batch(built_lib, cuda, [(a, b, g, 64, True)], params=p)
+    assert rc == _native.MPS_ERR_TIMEOUT
+    assert "expired" in _native.last_error()
+    rc, res, _ = run_batch(built_lib, cuda, [(a, b, g, 64, True)])
+    assert rc == 0, _native.last_error()
+    check_job((a, b, g, 64, True), res[0], 2)
