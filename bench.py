@@ -151,12 +151,16 @@ def _time_call(fn, min_seconds=0.02):
             return dt / reps
 
 
-def cpu_sample(circ, seed=123):
+def cpu_sample(circ, seed=123, budget=12.0):
     """The reference's CPU algorithm (NumPy oracle port: merge, LAPACK SVD,
     regauge; one-qudit contraction) timed on one gate of every distinct shape
-    of ``circ``, weighted by how often each shape occurs.  Returns (two-qudit
-    gates/s over the whole circuit, seconds spent timing, per-gate seconds of
-    the per-gate norm sweep the reference also runs, at the largest bond)."""
+    of ``circ``, weighted by how often each shape occurs.  A short first pass
+    estimates each shape's cost; the ``budget`` seconds are then split over the
+    shapes by their share of the whole circuit's CPU time and each shape is
+    timed again for its share.  Returns (two-qudit gates/s over the whole
+    circuit, seconds spent timing, per-gate seconds of the per-gate norm sweep
+    the reference also runs, at the largest bond, number of two-qudit shapes,
+    number of one-qudit shapes)."""
     from oracle.ref_mps import OracleMPS
     from mpsim_gb300.circuits import haar_random_matrix
     rng = np.random.default_rng(seed)
@@ -168,25 +172,31 @@ def cpu_sample(circ, seed=123):
         t = (rng.normal(size=shape) + 1j * rng.normal(size=shape)).astype(np.complex64)
         return t / np.sqrt(t.size)
 
-    total = 0.0
+    calls = []                                   # (count, fn)
     g2 = haar_random_matrix(2, d, 1000)
     for (cl, cm, cr), count in two.items():
         a, b = rnd((cl, d, cm)), rnd((cm, d, cr))
         o = OracleMPS(2, d, np.complex64)
 
-        def gate():
+        def gate(o=o, a=a, b=b):
             o.sites = [a, b]
             o.apply_two_qudit_gate(g2, 0, 1, maxsvals=circ.maxsvals)
-        total += count * _time_call(gate)
+        calls.append((count, gate))
     g1 = haar_random_matrix(1, d, 1001)
     for (cl, cr), count in one.items():
         o = OracleMPS(2, d, np.complex64)
         s = rnd((cl, d, cr))
 
-        def gate1():
+        def gate1(o=o, s=s):
             o.sites[0] = s
             o.apply_one_qudit_gate(g1, 0)
-        total += count * _time_call(gate1, 0.005)
+        calls.append((count, gate1))
+    est = [count * _time_call(fn, 0.005) for count, fn in calls]
+    spent = time.perf_counter() - t_start
+    left = max(budget - spent, 0.0)
+    total = 0.0
+    for (count, fn), e in zip(calls, est):
+        total += count * _time_call(fn, max(0.005, left * e / sum(est)))
     chi = max(c[1] for c in two)
     a = rnd((chi, d, chi))
 
@@ -205,11 +215,11 @@ def run_reference(args, rank, world):
     from mpsim_gb300 import circuits as C
     circ = C.workload(args.workload if args.workload in C.WORKLOADS else WORKLOAD)
     for _ in range(args.warmup):
-        cpu_sample(circ)
+        cpu_sample(circ, budget=2.0)
     rates = []
     t_all = time.perf_counter()
     for _ in range(args.steps):
-        rate, spent, norm_cost, n2, n1 = cpu_sample(circ)
+        rate, spent, norm_cost, n2, n1 = cpu_sample(circ, budget=10.0)
         rates.append(rate)
     total = time.perf_counter() - t_all
     value = float(np.mean(rates))
@@ -217,7 +227,7 @@ def run_reference(args, rank, world):
     sample = (f"NumPy oracle port of mpsim/core.py (merge, np.linalg.svd, regauge; one-qudit "
               f"contraction) timed on one gate of each of the {n2} two-qudit and {n1} one-qudit "
               f"shapes of the {circ.nqudits}-qubit depth-{circ.depth} circuit and weighted by their "
-              f"counts, {cores} host threads; excludes the per-gate norm sweep the reference runs "
+              f"counts, {spent:.1f}s of timing per step, {cores} host threads; excludes the per-gate norm sweep the reference runs "
               f"after every two-qudit gate (~{norm_cost:.3f}s per gate at chi=256)")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -479,6 +479,33 @@ class MPS:
         if norm is not None:
             self.renormalize(norm)
 
+    def _apply_one_qudit_layer(self, one_qudit) -> None:
+        """One-qudit gates on every site (``one_qudit``: (n, d, d)) in one
+        batched launch; non-unitary gates take the per-gate path."""
+        d, n = self._qudit_dimension, self._nqudits
+        if isinstance(one_qudit, (list, tuple)):
+            u = np.stack([np.asarray(gate_tensor(x)) for x in one_qudit])
+        else:
+            u = np.asarray(gate_tensor(one_qudit))
+        if u.shape != (n, d, d):
+            raise ValueError(f"one-qudit layer must have shape ({n}, {d}, {d})")
+        prod = np.einsum("nji,njk->nik", u.conj(), u)
+        if not np.allclose(prod, np.broadcast_to(np.identity(d), prod.shape), atol=1e-5):
+            for i in range(n):
+                self.apply_one_qudit_gate(u[i], i)
+            return
+        if not self.is_valid():
+            raise ValueError("MPS is invalid.")
+        g = torch.from_numpy(np.ascontiguousarray(u.astype(np.complex64))).to(self._device)
+        table = np.zeros(n, dtype=_native.JOB1_DTYPE)
+        for i, site in enumerate(self._sites):
+            table[i]["site"] = site.data_ptr()
+            table[i]["gate"] = g[i].data_ptr()
+            table[i]["chi_l"], table[i]["chi_r"] = int(site.shape[0]), int(site.shape[2])
+        jt = torch.from_numpy(table.view(np.uint8)).to(self._device)
+        _native.check(self._lib().mps_apply_1q_batch(self._stream(), ctypes.c_void_p(jt.data_ptr()),
+                                                     n, d))
+
     def apply_one_qudit_gate_to_all(self, gate) -> None:
         for i in range(self._nqudits):
             self.apply_one_qudit_gate(gate, i)
@@ -501,10 +528,19 @@ class MPS:
             raise ValueError(f"Gate edges have dimension {dims[0]} but should have MPS qudit "
                              f"dimension = {self._qudit_dimension}")
 
-    def _prepare_pair(self, gate, i, j, kwargs):
+    def _prepare_pair(self, gate, i, j, kwargs, checked=False):
         """Validate, flip, and return (G (d^2 x d^2) complex64, left, k, lc)
-        for an ADJACENT pair.  Mirrors core.py:1000-1033 and 1104-1130."""
-        self._check_two_qudit(gate, i, j)
+        for an ADJACENT pair.  Mirrors core.py:1000-1033 and 1104-1130.
+        ``checked``: the caller already verified that the MPS is valid."""
+        if checked:
+            if i not in range(self._nqudits) or j not in range(self._nqudits) or i == j:
+                raise ValueError(f"Input tensor indices={(i, j)} are out of bounds for an MPS on "
+                                 f"{self._nqudits} qudits.")
+            dims = tuple(int(x) for x in np.shape(gate_tensor(gate)))
+            if len(dims) != 4 or len(set(dims)) != 1 or dims[0] != self._qudit_dimension:
+                raise ValueError("Two qudit gate must be (d, d, d, d) with the MPS qudit dimension.")
+        else:
+            self._check_two_qudit(gate, i, j)
         d = self._qudit_dimension
         g = np.asarray(gate_tensor(gate)).reshape((d,) * 4)
         if j < i:
@@ -702,10 +738,11 @@ class MPS:
         ``two_qudit[p]`` (d^2 x d^2) on (pair_left[p], pair_left[p] + 1), the
         pairs disjoint -- the same result as applying the gates one by one."""
         if one_qudit is not None:
-            for i in range(self._nqudits):
-                self.apply_one_qudit_gate(one_qudit[i], i)
+            self._apply_one_qudit_layer(one_qudit)
         if two_qudit is None or len(pair_left) == 0:
             return
+        if not self.is_valid():
+            raise ValueError("MPS is not valid.")
         used = set()
         pairs = []
         for p, i in enumerate(pair_left):
@@ -714,7 +751,7 @@ class MPS:
                 raise ValueError("apply_layer pairs must be disjoint")
             used.update((i, i + 1))
             pairs.append(self._prepare_pair(np.asarray(two_qudit[p]).reshape((self._qudit_dimension,) * 4),
-                                            i, i + 1, kwargs))
+                                            i, i + 1, kwargs, checked=True))
         if self.track_norms:
             for pr in pairs:
                 self._run_pairs([pr])
@@ -731,11 +768,14 @@ class MPS:
         if one_qudit_dev is not None:
             if tuple(one_qudit_dev.shape) != (self._nqudits, d, d):
                 raise ValueError("one_qudit_dev must have shape (nqudits, d, d)")
-            lib = self._lib()
+            table = np.zeros(self._nqudits, dtype=_native.JOB1_DTYPE)
             for i, site in enumerate(self._sites):
-                _native.check(lib.mps_apply_1q(
-                    self._stream(), ctypes.c_void_p(site.data_ptr()), int(site.shape[0]), d,
-                    int(site.shape[2]), ctypes.c_void_p(one_qudit_dev[i].data_ptr())))
+                table[i]["site"] = site.data_ptr()
+                table[i]["gate"] = one_qudit_dev[i].data_ptr()
+                table[i]["chi_l"], table[i]["chi_r"] = int(site.shape[0]), int(site.shape[2])
+            jt = torch.from_numpy(table.view(np.uint8)).to(self._device)
+            _native.check(self._lib().mps_apply_1q_batch(
+                self._stream(), ctypes.c_void_p(jt.data_ptr()), self._nqudits, d))
         if two_qudit_dev is None or len(pair_left) == 0:
             return
         used = set()
