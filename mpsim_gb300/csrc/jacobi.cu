@@ -8,14 +8,18 @@
 //
 // Algorithm.  The C columns of X are split into nb blocks of BC columns
 // (zero-padded).  A sweep is nb-1 rounds of nb/2 disjoint block pairs
-// (circle-method round robin, one launch per round, one CTA per (block pair,
-// job)), so every pair of columns is rotated exactly once per sweep:
+// (circle-method round robin), so every pair of columns is rotated exactly
+// once per sweep.  One persistent launch runs a whole sweep: CTAs take
+// (round, job, block pair) items in round-major order and wait (bounded) for
+// the two blocks' previous round.
 //  * round 0 ("full" visit): the CTA stages its 2*BC columns in shared memory
 //    and rotates all pairs among them -- the intra-block pairs of every block
 //    (round 0's pairs cover each block once) and the first inter-block pairs;
 //  * rounds 1..nb-2 ("ring" visit): only the BC*BC inter-block pairs.  Warp w
-//    keeps home column I*BC+w in registers; the J columns travel warp to warp
-//    through shared memory, so each step moves one column per warp.
+//    keeps home column I*BC+w in registers and meets the J columns in turn;
+//    in the sweep kernel the J columns stay in shared memory and pass from
+//    warp to warp through per-column step counters (visit_ring_handoff); the
+//    per-round kernels pass them through double-buffered slots (visit_ring).
 // For a pair (x, q) with gamma = x^H q, alpha = |x|^2, beta = |q|^2 the
 // rotation zeroes gamma:
 //   zeta = (beta - alpha) / (2|gamma|), t = sign(zeta)/(|zeta| + sqrt(1+zeta^2)),
@@ -24,10 +28,10 @@
 // The tau form keeps c = 1 - s tau implicit: with an explicit c, tiny angles
 // round c up to exactly 1 and every such rotation grows the column norms; over
 // thousands of rotations that biases every singular value.  A pair is rotated
-// only when |gamma| > tol sqrt(alpha beta) (tol = 2^-24 max(8, sqrt(L)) by
-// default);
-// a sweep with no rotation in a job marks the job converged.  Column norms
-// are recomputed from the rotated data, so they do not drift.
+// only when |gamma|^2 > tol^2 alpha beta (tol = 2^-24 max(8, sqrt(L)) by
+// default); a sweep with no rotation in a job marks the job converged.
+// Column norms are recomputed from the data at every visit, so they do not
+// drift.
 //
 // V.  A job that is tall (m >= n) and left-canonical -- the default of
 // apply_two_qudit_gate -- needs only U = X_k / S: one Newton-Schulz step makes
@@ -51,24 +55,49 @@ namespace mps {
 namespace {
 
 struct Rot {
-    float s, tau, t;
+    float s, tau, t, ag;
     cf e;
 };
 
-// zeta and t set only the rotation angle, so fast divisions do; the unit
-// phase e and c (and tau, which fixes c = 1 - s tau) are kept correctly
-// rounded because their errors would make the rotation non-unitary.
-__device__ __forceinline__ Rot make_rot(float a, float b, cf gam, float ag) {
+// Squared cosine of the angle between two columns, |gamma|^2 / (a b).  A pair
+// rotates when it exceeds tol^2, and the per-job maximum of the same value
+// decides convergence, so a sweep that rotates nothing always ends the job.
+// Zero columns give 0; norms below the smallest normal float take IEEE
+// divisions (the fast ones flush them).
+__device__ __forceinline__ float pair_cos2(float g2, float a, float b) {
+    const float kMinNormal = 1.17549435e-38f;
+    if (a >= kMinNormal && b >= kMinNormal) return __fdividef(__fdividef(g2, a), b);
+    return (a > 0.f && b > 0.f) ? (g2 / a) / b : 0.f;
+}
+
+// Rotation parameters for g2 = |gamma|^2 > 0.  zeta and t set only the
+// angle, so fast divisions and an approximate square root do.  An error of
+// relative size eps in c or tau changes a rotated column's norm by about
+// eps s^2, so c comes from an approximate reciprocal square root refined by
+// one Newton step and tau from a fast division.  The unit phase e multiplies
+// a column at every rotation, however small the angle, so |e| must be 1 to
+// rounding: it uses the correctly rounded reciprocal square root, which also
+// gives |gamma|.
+__device__ __forceinline__ Rot make_rot(float a, float b, cf gam, float g2) {
+    const float inv = __frsqrt_rn(g2);
+    const float ag = g2 * inv;
     const float zeta = __fdividef(b - a, 2.f * ag);
     const float az = fabsf(zeta);
-    const float t = az > 1e10f ? __fdividef(0.5f, zeta)
-                               : copysignf(__fdividef(1.f, az + sqrtf(fmaf(zeta, zeta, 1.f))), zeta);
-    const float c = __frsqrt_rn(fmaf(t, t, 1.f));
+    float t;
+    if (az > 1e10f) {
+        t = __fdividef(0.5f, zeta);
+    } else {
+        const float w = fmaf(zeta, zeta, 1.f);           // >= 1
+        t = copysignf(__fdividef(1.f, az + w * rsqrtf(w)), zeta);
+    }
+    const float x = fmaf(t, t, 1.f);
+    float c = rsqrtf(x);
+    c = c * fmaf(-0.5f * x * c, c, 1.5f);                // Newton step for 1/sqrt(x)
     Rot r;
     r.t = t;
+    r.ag = ag;
     r.s = c * t;
-    r.tau = r.s / (1.f + c);
-    const float inv = __frsqrt_rn(cabs2(gam));
+    r.tau = __fdividef(r.s, 1.f + c);
     r.e = cmake(gam.x * inv, -gam.y * inv);
     return r;
 }
@@ -143,7 +172,7 @@ __device__ __forceinline__ void publish_offmax(float offmax, float* s_off, int n
 // cached it.
 template <int BC, int ROWS>
 __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, const TwoQGeom& g,
-                                           int j, int round, int pair, float tol, float2* smem,
+                                           int j, int round, int pair, float tol2, float2* smem,
                                            float* s_off) {
     if (g.done[j]) return;
     const JobShape sh = job_shape<BC>(jobs, j, g.d);
@@ -193,12 +222,11 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
         gam.x = warp_sum(gam.x);
         gam.y = warp_sum(gam.y);
         const float a = nrm[p], b = nrm[q];
-        const float ag = sqrtf(cabs2(gam));
-        const float den = sqrtf(a) * sqrtf(b);
-        const float rel = den > 0.f ? ag / den : 0.f;
-        offmax = fmaxf(offmax, rel);
-        if (rel > tol) {                        // warp-uniform (butterfly sums)
-            const Rot R = make_rot(a, b, gam, ag);
+        const float g2 = cabs2(gam);
+        const float r2 = pair_cos2(g2, a, b);
+        offmax = fmaxf(offmax, r2);
+        if (r2 > tol2) {                        // warp-uniform (butterfly sums)
+            const Rot R = make_rot(a, b, gam, g2);
             float na = 0.f, nq = 0.f;
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) {
@@ -237,10 +265,10 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
 
 template <int BC, int ROWS>
 __global__ void __launch_bounds__(BC * 32)
-full_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
+full_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol2) {
     extern __shared__ float2 smem[];
     __shared__ float s_off[BC];
-    visit_full<BC, ROWS>(jobs, g, blockIdx.y, round, blockIdx.x, tol, smem, s_off);
+    visit_full<BC, ROWS>(jobs, g, blockIdx.y, round, blockIdx.x, tol2, smem, s_off);
 }
 
 // ---------------------------------------------------------------------------
@@ -248,7 +276,7 @@ full_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
 // I*BC+w) and block J (visitors, passed to warp w+1 after every step).
 template <int BC, int ROWS>
 __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, const TwoQGeom& g,
-                                           int j, int round, int pair, float tol, float2* smem,
+                                           int j, int round, int pair, float tol2, float2* smem,
                                            float* s_off) {
     // Every slot column has exactly 32*ROWS rows (lslot == 32*ROWS) and rows
     // past the job's length are zero, so no row is predicated: zero rows stay
@@ -295,18 +323,17 @@ __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, 
         for (int i = 0; i < ROWS; ++i) cfma_conj(gam, hx[i], vx[i]);
         gam.x = warp_sum(gam.x);
         gam.y = warp_sum(gam.y);
-        const float ag = sqrtf(cabs2(gam));
-        const float den = sqrtf(hn) * sqrtf(vn);
-        const float rel = den > 0.f ? ag / den : 0.f;
-        offmax = fmaxf(offmax, rel);
-        if (rel > tol) {
-            const Rot R = make_rot(hn, vn, gam, ag);
+        const float g2 = cabs2(gam);
+        const float r2 = pair_cos2(g2, hn, vn);
+        offmax = fmaxf(offmax, r2);
+        if (r2 > tol2) {
+            const Rot R = make_rot(hn, vn, gam, g2);
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) apply_rot(R, hx[i], vx[i]);
             // closed-form norm update (Hestenes): |x'|^2 = |x|^2 - t|gamma|,
             // |q'|^2 = |q|^2 + t|gamma|; recompute when cancellation leaves
             // less than 1/16 of a norm (warp-uniform decision)
-            const float dn = R.t * ag;
+            const float dn = R.t * R.ag;
             float na = hn - dn, nq = vn + dn;
             if (na < 0.0625f * hn || nq < 0.0625f * vn) {
                 na = 0.f;
@@ -363,12 +390,148 @@ __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, 
     publish_offmax(offmax, s_off, BC, g.offmax + j);
 }
 
+// The same BC*BC pairs for the persistent sweep kernel, with the J columns
+// kept in shared memory instead of travelling warp to warp: at step s warp w
+// takes visitor (w - s) mod BC (the order of visit_ring), so visitor v passes
+// from warp w-1 (step s-1) to warp w (step s).  The hand-off is a per-visitor step counter in shared
+// memory that the owner advances after its last access, so a warp waits only
+// for its neighbour instead of for the whole CTA every step and the warps'
+// dot-product, angle and rotation phases overlap; a visitor that was not
+// rotated is not written back.  Each wait polls at most wait_limit times; on
+// expiry it sets *err and goes on without waiting (the call then reports a
+// timeout and its results are not used), so every warp still reaches the
+// CTA barriers.
+template <int BC, int ROWS>
+__device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict__ jobs,
+                                                   const TwoQGeom& g, int j, int round, int pair,
+                                                   float tol2, float2* smem, float* s_off,
+                                                   int* err, int wait_limit) {
+    if (g.done[j]) return;
+    const JobShape sh = job_shape<BC>(jobs, j, g.d);
+    if (sh.C < 2) return;
+    if (round >= sh.nb - 1 || pair >= sh.nb / 2) return;
+    int I, J;
+    tournament_pair(sh.nb, round, pair, I, J);
+    constexpr int LW = 32 * ROWS;
+    constexpr int W = 2 * BC;
+    static_assert((BC & (BC - 1)) == 0, "BC must be a power of two");
+    cf* X = g.X + (size_t)j * g.lslot * g.cslot;
+    cf* vis = smem;                             // [BC][LW]
+    cf* Qs = smem + (size_t)BC * LW;            // [W][W], column-major
+    float* visn = reinterpret_cast<float*>(Qs + W * W);   // [BC]
+    volatile int* ready = reinterpret_cast<volatile int*>(visn + BC);   // [BC]
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    cf hx[ROWS], vx[ROWS];
+    float hn = 0.f;
+    {
+        const cf* hs = X + (size_t)(I * BC + warp) * g.lslot;
+        const cf* vs = X + (size_t)(J * BC + warp) * g.lslot;
+        cf* vd = vis + (size_t)warp * LW;
+        float vn = 0.f;
+#pragma unroll
+        for (int i = 0; i < ROWS; ++i) {
+            hx[i] = __ldcg(hs + lane + 32 * i);
+            vx[i] = __ldcg(vs + lane + 32 * i);
+            vd[lane + 32 * i] = vx[i];
+            hn += cabs2(hx[i]);
+            vn += cabs2(vx[i]);
+        }
+        hn = warp_sum(hn);
+        vn = warp_sum(vn);
+        if (lane == 0) {
+            visn[warp] = vn;
+            ready[warp] = 0;
+        }
+    }
+    if (sh.track_v)
+        for (int e = tid; e < W * W; e += BC * 32)
+            Qs[e] = (e % W == e / W) ? cmake(1.f, 0.f) : cmake(0.f, 0.f);
+    __syncthreads();
+    float offmax = 0.f;
+    bool expired = false;
+    for (int step = 0; step < BC; ++step) {
+        const int v = (warp + BC - step) & (BC - 1);
+        cf* vcol = vis + (size_t)v * LW;
+        if (step > 0) {
+            // visitor v was processed by warp-1 at step-1; the vote keeps
+            // the poll count, and so the expiry, uniform across the warp
+            int polls = 0;
+            while (!expired && !__all_sync(0xffffffffu, ready[v] >= step)) {
+                if (++polls > wait_limit) expired = true;
+            }
+            __threadfence_block();
+#pragma unroll
+            for (int i = 0; i < ROWS; ++i) vx[i] = vcol[lane + 32 * i];
+        }
+        const float vn = visn[v];
+        cf gam = cmake(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < ROWS; ++i) cfma_conj(gam, hx[i], vx[i]);
+        gam.x = warp_sum(gam.x);
+        gam.y = warp_sum(gam.y);
+        const float g2 = cabs2(gam);
+        const float r2 = pair_cos2(g2, hn, vn);
+        offmax = fmaxf(offmax, r2);
+        if (r2 > tol2) {                        // warp-uniform (butterfly sums)
+            const Rot R = make_rot(hn, vn, gam, g2);
+#pragma unroll
+            for (int i = 0; i < ROWS; ++i) {
+                apply_rot(R, hx[i], vx[i]);
+                vcol[lane + 32 * i] = vx[i];
+            }
+            // closed-form norm update, recomputed on cancellation (as in
+            // visit_ring)
+            const float dn = R.t * R.ag;
+            float na = hn - dn, nq = vn + dn;
+            if (na < 0.0625f * hn || nq < 0.0625f * vn) {
+                na = 0.f;
+                nq = 0.f;
+#pragma unroll
+                for (int i = 0; i < ROWS; ++i) {
+                    na += cabs2(hx[i]);
+                    nq += cabs2(vx[i]);
+                }
+                na = warp_sum(na);
+                nq = warp_sum(nq);
+            }
+            hn = na;
+            if (lane == 0) visn[v] = nq;
+            if (sh.track_v && lane < W) {
+                cf qa = Qs[warp * W + lane], qb = Qs[(BC + v) * W + lane];
+                apply_rot(R, qa, qb);
+                Qs[warp * W + lane] = qa;
+                Qs[(BC + v) * W + lane] = qb;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            ready[v] = step + 1;
+        }
+    }
+    if (expired && lane == 0) atomicExch(err, 1);
+    __syncthreads();
+    {
+        cf* hd = X + (size_t)(I * BC + warp) * g.lslot;
+        cf* vd = X + (size_t)(J * BC + warp) * g.lslot;
+        const cf* vsrc = vis + (size_t)warp * LW;
+#pragma unroll
+        for (int i = 0; i < ROWS; ++i) {
+            hd[lane + 32 * i] = hx[i];
+            vd[lane + 32 * i] = vsrc[lane + 32 * i];
+        }
+    }
+    if (sh.track_v) update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
+    publish_offmax(offmax, s_off, BC, g.offmax + j);
+}
+
 template <int BC, int ROWS>
 __global__ void __launch_bounds__(BC * 32)
-ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol) {
+ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, float tol2) {
     extern __shared__ float2 smem[];
     __shared__ float s_off[BC];
-    visit_ring<BC, ROWS>(jobs, g, blockIdx.y, round, blockIdx.x, tol, smem, s_off);
+    visit_ring<BC, ROWS>(jobs, g, blockIdx.y, round, blockIdx.x, tol2, smem, s_off);
 }
 
 // ---------------------------------------------------------------------------
@@ -382,7 +545,7 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
 // the error flag and the CTA leaves, as do the others once they see it.
 template <int BC, int ROWS>
 __global__ void __launch_bounds__(BC * 32)
-sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol, int njobs, int rounds,
+sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int njobs, int rounds,
              int pairs, SweepSync sync) {
     extern __shared__ float2 smem[];
     __shared__ float s_off[BC];
@@ -428,8 +591,9 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol, int njo
             if (s_abort) return;
         }
         if (active) {
-            if (r == 0) visit_full<BC, ROWS>(jobs, g, j, r, p, tol, smem, s_off);
-            else visit_ring<BC, ROWS>(jobs, g, j, r, p, tol, smem, s_off);
+            if (r == 0) visit_full<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off);
+            else visit_ring_handoff<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off, sync.error,
+                                              sync.wait_limit);
             __syncthreads();
             if (threadIdx.x == 0) {
                 __threadfence();
@@ -441,12 +605,12 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol, int njo
     }
 }
 
-__global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol) {
+__global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol2) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= njobs) return;
     if (!g.done[j]) {
         const float o = g.offmax[j];
-        if (o > tol) atomicAdd(g.counter, 1);
+        if (o > tol2) atomicAdd(g.counter, 1);
         else g.done[j] = 1;
     }
     g.offmax[j] = 0.f;
@@ -948,7 +1112,7 @@ size_t ring_smem(int lw) {
 
 template <int BC, int ROWS>
 int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g, int round,
-                 float tol, int lw, cudaStream_t s) {
+                 float tol2, int lw, cudaStream_t s) {
     dim3 grid(pairs, njobs);
     if (round == 0) {
         static std::once_flag once;
@@ -956,7 +1120,7 @@ int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g
         if (prepare_kernel(full_visit_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
         const size_t smem = full_smem<BC>(lw);
         if (smem > (size_t)limit) return fail(MPS_ERR_ARG, "jacobi: merged matrix too long for shared memory");
-        full_visit_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol);
+        full_visit_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol2);
         MPS_LAUNCH_CHECK("full_visit_kernel");
     } else {
         static std::once_flag once;
@@ -964,7 +1128,7 @@ int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g
         if (prepare_kernel(ring_visit_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
         const size_t smem = ring_smem<BC>(lw);
         if (smem > (size_t)limit) return fail(MPS_ERR_ARG, "jacobi: merged matrix too long for shared memory");
-        ring_visit_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol);
+        ring_visit_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol2);
         MPS_LAUNCH_CHECK("ring_visit_kernel");
     }
     return MPS_OK;
@@ -972,7 +1136,7 @@ int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g
 
 template <int BC, int ROWS>
 int launch_sweep(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const TwoQGeom& g,
-                 float tol, int lw, const SweepSync& sync, cudaStream_t s) {
+                 float tol2, int lw, const SweepSync& sync, cudaStream_t s) {
     static std::once_flag once;
     static int limit = 0, rc = MPS_OK, ctas = 0;
     if (prepare_kernel(sweep_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
@@ -989,7 +1153,7 @@ int launch_sweep(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const
     const int items = rounds * njobs * pairs;
     const int grid = items < ctas ? items : ctas;
     if (grid <= 0) return MPS_OK;
-    sweep_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, tol, njobs, rounds, pairs, sync);
+    sweep_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, tol2, njobs, rounds, pairs, sync);
     MPS_LAUNCH_CHECK("sweep_kernel");
     return MPS_OK;
 }
@@ -1128,6 +1292,7 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     // tol s_k / gap at the truncation cut -- stays close to what a
     // backward-stable complex64 SVD gives.
     if (!(tol > 0.f)) tol = 5.9604645e-8f * fmaxf(8.f, sqrtf((float)lo.lslot));
+    const float tol2 = tol * tol;     // the kernels compare squared cosines
     const int lw = lo.lslot;
     int bc = 16;
     (void)pick_visit(lw, &bc);
@@ -1186,9 +1351,9 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
             MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, 2 * sizeof(int), s));
             MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
                                            (size_t)njobs * lo.nbmax * sizeof(int), s));
-            rc = sweep(jobs, njobs, rounds, pairs, g, tol, lw, sync, s);
+            rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, s);
             if (rc) return rc;
-            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol);
+            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
             MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
@@ -1336,6 +1501,7 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
         tol = params->tol;
     }
     if (!(tol > 0.f)) tol = 5.9604645e-8f * fmaxf(8.f, sqrtf((float)lo.lslot));
+    const float tol2 = tol * tol;     // the kernels compare squared cosines
     const int lw = lo.lslot;
     int bc = 16;
     visit_fn visit = pick_visit(lw, &bc);
@@ -1380,10 +1546,10 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
                 t = g.V; g.V = V2; V2 = t;
             }
             for (int r = 0; r < rounds; ++r) {
-                rc = visit(jobs, njobs, pairs, g, r, tol, lw, s);
+                rc = visit(jobs, njobs, pairs, g, r, tol2, lw, s);
                 if (rc) return rc;
             }
-            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol);
+            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
             MPS_CUDA_CHECK(cudaMemcpyAsync(host_counter, g.counter, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
