@@ -32,6 +32,31 @@ __host__ __device__ __forceinline__ void cfma_conj(cf& acc, cf a, cf b) {
     acc.y = fmaf(a.x, b.y, fmaf(-a.y, b.x, acc.y));
 }
 
+// Shared-memory mbarrier (CTA scope): init with an arrival count, arrive
+// (release), and a bounded try_wait on a phase parity (acquire) that suspends
+// the calling thread for up to about suspend_ns while the phase is open.
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(a)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity, unsigned suspend_ns) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity), "r"(suspend_ns)
+        : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -18,15 +18,15 @@
 //  * rounds 1..nb-2 ("ring" visit): only the BC*BC inter-block pairs.  Warp w
 //    keeps home column I*BC+w in registers and meets the J columns in turn;
 //    in the sweep kernel the J columns stay in shared memory and pass from
-//    warp to warp through per-column step counters (visit_ring_handoff); the
+//    warp to warp through per-column mbarriers (visit_ring_handoff); the
 //    per-round kernels pass them through double-buffered slots (visit_ring).
 // For a pair (x, q) with gamma = x^H q, alpha = |x|^2, beta = |q|^2 the
 // rotation zeroes gamma:
 //   zeta = (beta - alpha) / (2|gamma|), t = sign(zeta)/(|zeta| + sqrt(1+zeta^2)),
-//   c = 1/sqrt(1+t^2), s = c t, tau = s/(1+c), e = conj(gamma)/|gamma|, y = e q,
-//   x <- x - s (y + tau x),   q <- y + s (x - tau y).
-// The tau form keeps c = 1 - s tau implicit: with an explicit c, tiny angles
-// round c up to exactly 1 and every such rotation grows the column norms; over
+//   c = 1/sqrt(1+t^2), s = c t, sigma = s conj(gamma)/|gamma|, tp = s^2/(1+c),
+//   x <- x - (tp x + sigma q),   q <- q + (conj(sigma) x - tp q).
+// Keeping c implicit as 1 - tp matters: with an explicit c, tiny angles round
+// c up to exactly 1 and every such rotation grows the column norms; over
 // thousands of rotations that biases every singular value.  A pair is rotated
 // only when |gamma|^2 > tol^2 alpha beta (tol = 2^-24 max(8, sqrt(L)) by
 // default); a sweep with no rotation in a job marks the job converged.
@@ -54,11 +54,6 @@ namespace mps {
 
 namespace {
 
-struct Rot {
-    float s, tau, t, ag;
-    cf e;
-};
-
 // Squared cosine of the angle between two columns, |gamma|^2 / (a b).  A pair
 // rotates when it exceeds tol^2, and the per-job maximum of the same value
 // decides convergence, so a sweep that rotates nothing always ends the job.
@@ -70,44 +65,60 @@ __device__ __forceinline__ float pair_cos2(float g2, float a, float b) {
     return (a > 0.f && b > 0.f) ? (g2 / a) / b : 0.f;
 }
 
-// Rotation parameters for g2 = |gamma|^2 > 0.  zeta and t set only the
-// angle, so fast divisions and an approximate square root do.  An error of
-// relative size eps in c or tau changes a rotated column's norm by about
-// eps s^2, so c comes from an approximate reciprocal square root refined by
-// one Newton step and tau from a fast division.  The unit phase e multiplies
-// a column at every rotation, however small the angle, so |e| must be 1 to
-// rounding: it uses the correctly rounded reciprocal square root, which also
-// gives |gamma|.
+// The rotation of a pair in the form
+//   x <- x - (tp x + sigma q),   q <- q + (conj(sigma) x - tp q),
+// sigma = s conj(gamma)/|gamma|, tp = 1 - c = s^2 / (1 + c): the complex
+// Jacobi rotation [[c, -sigma], [conj(sigma), c]], with c kept implicit as
+// 1 - tp (see the file comment).  It equals the rotation with the unit phase
+// e = conj(gamma)/|gamma| applied to q (q <- e q + ...) followed by conj(e)
+// on the new q, which changes no norm and no orthogonality.  dn = t |gamma|
+// is the norm transfer: |x'|^2 = a - dn, |q'|^2 = b + dn.
+struct Rot {
+    float tp, dn;
+    cf sigma;
+};
+
+// Rotation parameters for g2 = |gamma|^2 > 0 from quantities scaled by
+// 1/(a+b) (no overflow or underflow for any representable norms):
+// t = sign(b-a) 2|gamma| / (|b-a| + sqrt((b-a)^2 + 4|gamma|^2)),
+// c = 1/sqrt(1+t^2) (approximate reciprocal square root refined by one
+// Newton step), s = c t.  |sigma|^2 and tp come from the same c^2 t^2, so
+// rounding perturbs a rotated column's norm by a few ulps times s^2 only.
 __device__ __forceinline__ Rot make_rot(float a, float b, cf gam, float g2) {
-    const float inv = __frsqrt_rn(g2);
-    const float ag = g2 * inv;
-    const float zeta = __fdividef(b - a, 2.f * ag);
-    const float az = fabsf(zeta);
-    float t;
-    if (az > 1e10f) {
-        t = __fdividef(0.5f, zeta);
-    } else {
-        const float w = fmaf(zeta, zeta, 1.f);           // >= 1
-        t = copysignf(__fdividef(1.f, az + w * rsqrtf(w)), zeta);
-    }
-    const float x = fmaf(t, t, 1.f);
+    const float ab = a + b;
+    const float u = ab >= 1e-30f ? __fdividef(1.f, ab) : 1.f / ab;
+    const float p = b - a;
+    const float ph = p * u;                              // in [-1, 1]
+    const float gh = (g2 * u) * u;                       // in (0, 1/4]
+    const float h = fmaf(ph, ph, 4.f * gh);
+    const float th = __fdividef(2.f, fabsf(ph) + h * rsqrtf(h));   // |t| / (|gamma| u)
+    const float t2 = gh * th * th;                       // t^2 <= 1
+    const float x = 1.f + t2;
     float c = rsqrtf(x);
     c = c * fmaf(-0.5f * x * c, c, 1.5f);                // Newton step for 1/sqrt(x)
+    const float sg = p >= 0.f ? 1.f : -1.f;
+    const float k = c * sg * u * th;                     // sigma = k conj(gamma)
     Rot r;
-    r.t = t;
-    r.ag = ag;
-    r.s = c * t;
-    r.tau = __fdividef(r.s, 1.f + c);
-    r.e = cmake(gam.x * inv, -gam.y * inv);
+    r.sigma = cmake(k * gam.x, -k * gam.y);
+    r.tp = __fdividef(c * c * t2, 1.f + c);
+    r.dn = sg * g2 * u * th;
     return r;
 }
 
 __device__ __forceinline__ void apply_rot(const Rot& r, cf& x, cf& q) {
-    const cf y = cmul(r.e, q);
-    const cf nx = csub(x, cscale(cadd(y, cscale(x, r.tau)), r.s));
-    const cf ny = cadd(y, cscale(csub(x, cscale(y, r.tau)), r.s));
-    x = nx;
-    q = ny;
+    const float sr = r.sigma.x, si = r.sigma.y, tp = r.tp;
+    float nxr = fmaf(-tp, x.x, x.x), nxi = fmaf(-tp, x.y, x.y);
+    float nqr = fmaf(-tp, q.x, q.x), nqi = fmaf(-tp, q.y, q.y);
+    nxr = fmaf(-sr, q.x, nxr);
+    nxi = fmaf(-sr, q.y, nxi);
+    nqr = fmaf(sr, x.x, nqr);
+    nqi = fmaf(sr, x.y, nqi);
+    nxr = fmaf(si, q.y, nxr);
+    nxi = fmaf(-si, q.x, nxi);
+    nqr = fmaf(si, x.y, nqr);
+    nqi = fmaf(-si, x.x, nqi);
+    x = cmake(nxr, nxi);
+    q = cmake(nqr, nqi);
 }
 
 struct JobShape {
@@ -210,6 +221,7 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
         tournament_pair(W, step, warp, p, q);
         cf* cp = Xs + (size_t)p * Lw;
         cf* cq = Xs + (size_t)q * Lw;
+        const float a = nrm[p], b = nrm[q];
         cf xp[ROWS], xq[ROWS];
         cf gam = cmake(0.f, 0.f);
 #pragma unroll
@@ -221,7 +233,6 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
         }
         gam.x = warp_sum(gam.x);
         gam.y = warp_sum(gam.y);
-        const float a = nrm[p], b = nrm[q];
         const float g2 = cabs2(gam);
         const float r2 = pair_cos2(g2, a, b);
         offmax = fmaxf(offmax, r2);
@@ -333,7 +344,7 @@ __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, 
             // closed-form norm update (Hestenes): |x'|^2 = |x|^2 - t|gamma|,
             // |q'|^2 = |q|^2 + t|gamma|; recompute when cancellation leaves
             // less than 1/16 of a norm (warp-uniform decision)
-            const float dn = R.t * R.ag;
+            const float dn = R.dn;
             float na = hn - dn, nq = vn + dn;
             if (na < 0.0625f * hn || nq < 0.0625f * vn) {
                 na = 0.f;
@@ -393,19 +404,30 @@ __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, 
 // The same BC*BC pairs for the persistent sweep kernel, with the J columns
 // kept in shared memory instead of travelling warp to warp: at step s warp w
 // takes visitor (w - s) mod BC (the order of visit_ring), so visitor v passes
-// from warp w-1 (step s-1) to warp w (step s).  The hand-off is a per-visitor step counter in shared
-// memory that the owner advances after its last access, so a warp waits only
-// for its neighbour instead of for the whole CTA every step and the warps'
-// dot-product, angle and rotation phases overlap; a visitor that was not
-// rotated is not written back.  Each wait polls at most wait_limit times; on
-// expiry it sets *err and goes on without waiting (the call then reports a
-// timeout and its results are not used), so every warp still reaches the
-// CTA barriers.
+// from warp w-1 (step s-1) to warp w (step s).  The hand-off is one
+// mbarrier per (step, visitor), bars[s * BC + v] with arrival count 1: the
+// owner at step s arrives after its last access and the owner at step s+1
+// waits on it, suspended in hardware rather than spinning, so a warp waits
+// only for its neighbour instead of for the whole CTA every step and the
+// warps' dot-product, angle and rotation phases overlap.  (One barrier per
+// visitor would not do: a warp may reach step s while the visitor's step s-2
+// arrival is still missing, and a parity wait cannot tell that phase from the
+// awaited one.)  Each barrier completes exactly one phase per visit, so the
+// phase awaited is the parity of the number of ring visits this CTA has made,
+// which the caller keeps in `parity` and this function flips.  A visitor that
+// was not rotated is not written back to shared memory, and a visit that
+// rotated nothing writes nothing back to global memory.  Each wait gives up after kHandoffTries suspended tries;
+// then it sets *err and goes on without waiting (the call reports a timeout
+// and its results are not used), so every warp still reaches the CTA
+// barriers.
+constexpr int kHandoffTries = 1 << 18;
+constexpr unsigned kHandoffSuspendNs = 1000;
+
 template <int BC, int ROWS>
 __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict__ jobs,
                                                    const TwoQGeom& g, int j, int round, int pair,
                                                    float tol2, float2* smem, float* s_off,
-                                                   int* err, int wait_limit) {
+                                                   uint64_t* bars, unsigned& parity, int* err) {
     if (g.done[j]) return;
     const JobShape sh = job_shape<BC>(jobs, j, g.d);
     if (sh.C < 2) return;
@@ -419,7 +441,6 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
     cf* vis = smem;                             // [BC][LW]
     cf* Qs = smem + (size_t)BC * LW;            // [W][W], column-major
     float* visn = reinterpret_cast<float*>(Qs + W * W);   // [BC]
-    volatile int* ready = reinterpret_cast<volatile int*>(visn + BC);   // [BC]
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     cf hx[ROWS], vx[ROWS];
@@ -439,28 +460,26 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
         }
         hn = warp_sum(hn);
         vn = warp_sum(vn);
-        if (lane == 0) {
-            visn[warp] = vn;
-            ready[warp] = 0;
-        }
+        if (lane == 0) visn[warp] = vn;
     }
     if (sh.track_v)
         for (int e = tid; e < W * W; e += BC * 32)
             Qs[e] = (e % W == e / W) ? cmake(1.f, 0.f) : cmake(0.f, 0.f);
     __syncthreads();
     float offmax = 0.f;
-    bool expired = false;
+    bool expired = false, rotated = false;
     for (int step = 0; step < BC; ++step) {
         const int v = (warp + BC - step) & (BC - 1);
         cf* vcol = vis + (size_t)v * LW;
         if (step > 0) {
             // visitor v was processed by warp-1 at step-1; the vote keeps
-            // the poll count, and so the expiry, uniform across the warp
-            int polls = 0;
-            while (!expired && !__all_sync(0xffffffffu, ready[v] >= step)) {
-                if (++polls > wait_limit) expired = true;
+            // the try count, and so the expiry, uniform across the warp
+            uint64_t* bar = bars + (step - 1) * BC + v;
+            int tries = 0;
+            while (!expired &&
+                   !__all_sync(0xffffffffu, mbar_try_wait(bar, parity, kHandoffSuspendNs))) {
+                if (++tries > kHandoffTries) expired = true;
             }
-            __threadfence_block();
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) vx[i] = vcol[lane + 32 * i];
         }
@@ -482,7 +501,7 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
             }
             // closed-form norm update, recomputed on cancellation (as in
             // visit_ring)
-            const float dn = R.t * R.ag;
+            const float dn = R.dn;
             float na = hn - dn, nq = vn + dn;
             if (na < 0.0625f * hn || nq < 0.0625f * vn) {
                 na = 0.f;
@@ -496,6 +515,7 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
                 nq = warp_sum(nq);
             }
             hn = na;
+            rotated = true;
             if (lane == 0) visn[v] = nq;
             if (sh.track_v && lane < W) {
                 cf qa = Qs[warp * W + lane], qb = Qs[(BC + v) * W + lane];
@@ -505,14 +525,12 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
             }
         }
         __syncwarp();
-        if (lane == 0) {
-            __threadfence_block();
-            ready[v] = step + 1;
-        }
+        if (lane == 0 && step + 1 < BC) mbar_arrive(bars + step * BC + v);
     }
+    parity ^= 1u;
     if (expired && lane == 0) atomicExch(err, 1);
-    __syncthreads();
-    {
+    const bool any = __syncthreads_or(rotated ? 1 : 0) != 0;
+    if (any) {
         cf* hd = X + (size_t)(I * BC + warp) * g.lslot;
         cf* vd = X + (size_t)(J * BC + warp) * g.lslot;
         const cf* vsrc = vis + (size_t)warp * LW;
@@ -522,7 +540,7 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
             vd[lane + 32 * i] = vsrc[lane + 32 * i];
         }
     }
-    if (sh.track_v) update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
+    if (sh.track_v && any) update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
     publish_offmax(offmax, s_off, BC, g.offmax + j);
 }
 
@@ -550,8 +568,14 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
     extern __shared__ float2 smem[];
     __shared__ float s_off[BC];
     __shared__ int s_item, s_abort;
+    // ring hand-off barriers, one per (step < BC-1, visitor); see
+    // visit_ring_handoff
+    __shared__ __align__(8) uint64_t s_bar[(BC - 1) * BC];
+    unsigned parity = 0;
     const int per_round = njobs * pairs;
     const int total = rounds * per_round;
+    // the loop's first barrier orders the initialisation before any use
+    for (int b = threadIdx.x; b < (BC - 1) * BC; b += blockDim.x) mbar_init(&s_bar[b], 1);
     for (;;) {
         if (threadIdx.x == 0) {
             s_item = atomicAdd(sync.next_item, 1);
@@ -592,8 +616,8 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
         }
         if (active) {
             if (r == 0) visit_full<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off);
-            else visit_ring_handoff<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off, sync.error,
-                                              sync.wait_limit);
+            else visit_ring_handoff<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off, s_bar, parity,
+                                              sync.error);
             __syncthreads();
             if (threadIdx.x == 0) {
                 __threadfence();
