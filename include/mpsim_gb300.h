@@ -41,10 +41,16 @@ extern "C" {
 
 typedef struct { float re, im; } mps_c64;
 
+/* mps_2q_job.flags: the job is the truncated SVD of a given matrix (a points
+ * to theta itself, (chi_l*d) x (d*chi_r) row-major; b, gate and chi_m are
+ * unused).  The plain SVD that from_wavefunction and the orthonormalisation
+ * of one site need (mpsim/core.py:245-328, 847-937). */
+#define MPS_JOB_THETA_GIVEN 1
+
 /* One two-qudit gate on adjacent sites (left site a, right site b).
  * 88 bytes, naturally aligned; the Python side mirrors it field by field. */
 typedef struct {
-    const mps_c64* a;      /* (chi_l, d, chi_m)                            */
+    const mps_c64* a;      /* (chi_l, d, chi_m), or theta (see flags)      */
     const mps_c64* b;      /* (chi_m, d, chi_r)                            */
     const mps_c64* gate;   /* (d*d, d*d) row-major G[(a'b'),(ab)]          */
     mps_c64* a_out;        /* (chi_l, d, k): new left site                 */
@@ -55,7 +61,7 @@ typedef struct {
     int32_t chi_l, chi_m, chi_r;
     int32_t k;             /* kept count, 0 <= k <= min(chi_l*d, d*chi_r)  */
     int32_t keep_left_canonical; /* 1: left=U, right=S.V^H; 0: U.S, V^H   */
-    int32_t pad0;
+    int32_t flags;         /* MPS_JOB_* bits; 0 for a gate on two sites    */
 } mps_2q_job;
 
 /* Solver controls for the Jacobi SVD (zero fields take the defaults). */
@@ -165,6 +171,33 @@ int mps_amplitudes(void* stream, const mps_c64* const* sites, const int* chis,
  * (to/norm)^(1/n)) and MPS.dagger (core.py:502-505, conj every site). */
 int mps_scale(void* stream, mps_c64* site, size_t count, float alpha_re,
               float alpha_im, int conj);
+
+/* Strided batched complex GEMM on the device: for z < max(batch, 1),
+ *   C[z](i, j) = sum_t opA(i, t) opB(t, j),  0 <= i < m, 0 <= j < n, t < k,
+ * with opA(i, t) = a[z*bsa + i*sam + t*sak] (conjugated when conj_a) and
+ * likewise b (sbk, sbn, conj_b) and c (scm, scn; overwritten).  The
+ * contractions the reference performs with TensorNetwork for the
+ * environment sweeps of MPS.reduced_density_matrix (mpsim/core.py:596-653)
+ * and for folding S.V^H or U.S into a neighbour after
+ * orthonormalize_right_edge_of / orthonormalize_left_edge_of
+ * (core.py:884-887, 933-937) use this. */
+int mps_cgemm(void* stream, int m, int n, int k, const mps_c64* a, long long sam,
+              long long sak, int conj_a, const mps_c64* b, long long sbk,
+              long long sbn, int conj_b, mps_c64* c, long long scm, long long scn,
+              int batch, long long bsa, long long bsb, long long bsc);
+
+/* Workspace for mps_site_marginals: every left environment plus two
+ * right environments and two (chi, d, chi) scratch tensors. */
+size_t mps_marginals_workspace_bytes(const int* chis, int n, int d);
+
+/* The diagonal of every single-site reduced density matrix,
+ * probs_host[i*d + x] = <psi| (|x><x| on site i) |psi> (not normalised), in
+ * one pass of left environments and one of right environments.  Blocks until
+ * done.  Replaces reduced_density_matrix(i).diagonal().real as
+ * MPS._sample uses it (mpsim/core.py:655-667, 596-653). */
+int mps_site_marginals(void* stream, const mps_c64* const* sites, const int* chis,
+                       int n, int d, void* workspace, size_t workspace_bytes,
+                       float* probs_host);
 
 #ifdef __cplusplus
 }

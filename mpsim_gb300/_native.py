@@ -26,6 +26,7 @@ NOALLOC_SCRATCH_BYTES = 32 << 20       # MPS_NOALLOC_SCRATCH_BYTES
 
 STATUS_NOT_CONVERGED = 1
 STATUS_NONFINITE = 2
+JOB_THETA_GIVEN = 1        # mps_2q_job.flags: a holds theta itself
 
 # mps_2q_job, field for field (88 bytes).
 JOB_DTYPE = np.dtype([
@@ -33,7 +34,7 @@ JOB_DTYPE = np.dtype([
     ("a_out", np.uint64), ("b_out", np.uint64), ("svals", np.uint64),
     ("discarded", np.uint64), ("status", np.uint64),
     ("chi_l", np.int32), ("chi_m", np.int32), ("chi_r", np.int32),
-    ("k", np.int32), ("keep_left_canonical", np.int32), ("pad0", np.int32),
+    ("k", np.int32), ("keep_left_canonical", np.int32), ("flags", np.int32),
 ])
 assert JOB_DTYPE.itemsize == 88
 
@@ -53,6 +54,7 @@ class SvdParams(ctypes.Structure):
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _SZ = ctypes.c_size_t
+_LL = ctypes.c_longlong
 SIGNATURES = {
     "mps_version": (_I, []),
     "mps_last_error": (ctypes.c_char_p, []),
@@ -67,6 +69,10 @@ SIGNATURES = {
     "mps_wavefunction": (_I, [_P, _P, _P, _I, _I, _P, _P, _SZ]),
     "mps_amplitudes": (_I, [_P, _P, _P, _I, _I, _P, _I, _P, _P, _SZ]),
     "mps_scale": (_I, [_P, _P, _SZ, ctypes.c_float, ctypes.c_float, _I]),
+    "mps_cgemm": (_I, [_P, _I, _I, _I, _P, _LL, _LL, _I, _P, _LL, _LL, _I, _P, _LL, _LL, _I,
+                       _LL, _LL, _LL]),
+    "mps_marginals_workspace_bytes": (_SZ, [_P, _I, _I]),
+    "mps_site_marginals": (_I, [_P, _P, _P, _I, _I, _P, _SZ, _P]),
 }
 
 _lock = threading.Lock()

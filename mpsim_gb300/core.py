@@ -19,9 +19,13 @@ Differences from the reference, all deliberate:
   own two sites;
 * ``get_node(s)`` return host copies (TensorNetwork-like nodes with the
   reference's initial axis order: physical axis first);
-* non-unitary one-qudit gates with orthonormalisation, sampling, reduced
-  density matrices and ``from_wavefunction`` are outside this build's hot
-  path and raise NotImplementedError.
+* ``from_wavefunction`` returns the reference's state in the left-canonical
+  gauge (TensorNetwork's split_node puts sqrt(S) on both sides) and takes
+  at most d^(nqudits-1) = 1792 amplitudes per row of its first split (the
+  Jacobi kernel's register-held column length: 11 qubits, 7 qutrits);
+* ``sample`` draws from the same single-site marginals with the same NumPy
+  global-RNG calls as the reference, computing all marginals in one device
+  pass instead of one full contraction per site and sample.
 """
 
 from __future__ import annotations
@@ -125,6 +129,72 @@ class _Workspace:
 
 
 _WS = _Workspace()
+
+
+# Longest merged matrix the Jacobi kernel takes (rows held in registers).
+MAX_SVD_LENGTH = 1792
+
+
+def _cgemm(lib, stream, m, n, k, a, a_off, sam, sak, conj_a, b, b_off, sbk, sbn, conj_b,
+           c, c_off, scm, scn, batch=1, bsa=0, bsb=0, bsc=0):
+    """mps_cgemm on torch complex64 tensors; *_off are element offsets."""
+    for z0 in range(0, max(batch, 1), 65535):
+        nb = min(65535, max(batch, 1) - z0)
+        _native.check(lib.mps_cgemm(
+            stream, m, n, k,
+            ctypes.c_void_p(a.data_ptr() + 8 * (a_off + z0 * bsa)), sam, sak, int(conj_a),
+            ctypes.c_void_p(b.data_ptr() + 8 * (b_off + z0 * bsb)), sbk, sbn, int(conj_b),
+            ctypes.c_void_p(c.data_ptr() + 8 * (c_off + z0 * bsc)), scm, scn, nb, bsa, bsb, bsc))
+
+
+def _given_svd(device, stream, mat, left_canonical: bool):
+    """Thin SVD of a device matrix ``mat`` (m x n complex64, row-major) with
+    the two-qudit kernel's given-matrix jobs (MPS_JOB_THETA_GIVEN, d = 1), keeping all
+    r = min(m, n) values.  Returns (left (m, r), right (r, n), singular values
+    (r,) float32 on the host): left = U, right = S V^H when left_canonical,
+    else left = U S, right = V^H."""
+    lib = _native.load()
+    m, n = (int(x) for x in mat.shape)
+    if max(m, n) > MAX_SVD_LENGTH:
+        raise NotImplementedError(
+            f"a {m} x {n} matrix is longer than the {MAX_SVD_LENGTH} rows the Jacobi SVD kernel "
+            f"holds")
+    r = min(m, n)
+    mat = mat.contiguous()
+    a_out = torch.empty((m, 1, r), dtype=torch.complex64, device=device)
+    b_out = torch.empty((r, 1, n), dtype=torch.complex64, device=device)
+    sv = torch.zeros(max(r, 1), dtype=torch.float32, device=device)
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    table = np.zeros(1, dtype=_native.JOB_DTYPE)
+    row = table[0]
+    row["a"], row["b"], row["gate"] = mat.data_ptr(), 0, 0
+    row["flags"] = _native.JOB_THETA_GIVEN
+    row["a_out"] = a_out.data_ptr() if a_out.numel() else 0
+    row["b_out"] = b_out.data_ptr() if b_out.numel() else 0
+    row["svals"], row["status"] = sv.data_ptr(), status.data_ptr()
+    row["chi_l"], row["chi_m"], row["chi_r"], row["k"] = m, n, n, r
+    row["keep_left_canonical"] = 1 if left_canonical else 0
+    jobs = torch.from_numpy(table.view(np.uint8)).to(device)
+    nbytes = lib.mps_2q_workspace_bytes(1, m, n, 1)
+    ws = _WS.get(device, nbytes, "2q")
+    rc = lib.mps_apply_2q_batch(stream, ctypes.c_void_p(jobs.data_ptr()), 1, m, n, 1,
+                                ctypes.c_void_p(ws.data_ptr()), ws.numel(),
+                                ctypes.byref(_native.SvdParams()))
+    if rc == _native.MPS_ERR_NOT_CONVERGED:
+        warnings.warn("mpsim_gb300: " + _native.last_error(), RuntimeWarning)
+    elif rc != _native.MPS_OK:
+        raise _native.NativeError(rc, _native.last_error())
+    return a_out.view(m, r), b_out.view(r, n), sv.cpu().numpy()[:r]
+
+
+def kept_by_truncation_error(svals: np.ndarray, max_truncation_err: float) -> int:
+    """Values TensorNetwork 0.2.1's split_node_full_svd keeps under
+    max_truncation_err (what mpsim/core.py:876-881, 926-931 ask for): count of
+    sqrt(cumsum(s[::-1]^2)) above the bound, i.e. the largest values whose
+    dropped tail has norm <= the bound (computed in the values' dtype)."""
+    s = np.asarray(svals)
+    errs = np.sqrt(np.cumsum(np.square(s[::-1])))
+    return int(np.count_nonzero(errs > max_truncation_err))
 
 
 def _ptr_array(tensors):
@@ -427,21 +497,174 @@ class MPS:
         other.apply(observable)
         return self.inner_product(other).real
 
-    def reduced_density_matrix(self, node_indices):
-        raise NotImplementedError("reduced_density_matrix is outside this build's scope")
+    def reduced_density_matrix(self, node_indices) -> np.ndarray:
+        """rho[(ket digits), (bra digits)] on ``node_indices`` (in that order),
+        every other site traced out (core.py:596-653); not normalised.  One
+        left-to-right environment sweep on the device: E[b, l, l'] with b the
+        digits of the sites kept so far, two batched complex GEMMs per site."""
+        try:
+            node_indices = iter(node_indices)
+        except TypeError:
+            node_indices = [node_indices]
+        node_indices = tuple(node_indices)
+        if len(set(node_indices)) < len(node_indices):
+            raise ValueError("Node indices contains duplicates.")
+        if min(node_indices) < 0 or max(node_indices) > self._nqudits - 1:
+            raise IndexError("One or more invalid node indices.")
+        d, dev = self._qudit_dimension, self._device
+        lib, stream = self._lib(), self._stream()
+        kept = sorted(node_indices)
+        keep_set = set(kept)
+        E = torch.ones((1, 1, 1), dtype=torch.complex64, device=dev)
+        nb = 1
+        for i, A in enumerate(self._sites):
+            cl, _, cr = (int(x) for x in A.shape)
+            # F[b, l', (a, r)] = sum_l E[b, l, l'] A[l, (a, r)]
+            F = torch.empty((nb, cl, d, cr), dtype=torch.complex64, device=dev)
+            _cgemm(lib, stream, cl, d * cr, cl, E, 0, 1, cl, 0, A, 0, d * cr, 1, 0,
+                   F, 0, d * cr, 1, nb, cl * cl, 0, cl * d * cr)
+            if i in keep_set:
+                # E'[b, a, a', r, r'] = sum_l' F[b, l', a, r] conj(A[l', a', r'])
+                E = torch.empty((nb, d, d, cr, cr), dtype=torch.complex64, device=dev)
+                for a in range(d):
+                    for a2 in range(d):
+                        _cgemm(lib, stream, cr, cr, cl, F, a * cr, 1, d * cr, 0,
+                               A, a2 * cr, d * cr, 1, 1, E, (a * d + a2) * cr * cr, cr, 1,
+                               nb, cl * d * cr, 0, d * d * cr * cr)
+                nb *= d * d
+                E = E.view(nb, cr, cr)
+            else:
+                # E'[b, r, r'] = sum_(l', a) F[b, (l', a), r] conj(A[(l', a), r'])
+                E = torch.empty((nb, cr, cr), dtype=torch.complex64, device=dev)
+                _cgemm(lib, stream, cr, cr, cl * d, F, 0, 1, cr, 0, A, 0, cr, 1, 1,
+                       E, 0, cr, 1, nb, cl * d * cr, 0, cr * cr)
+        k = len(kept)
+        vals = E.reshape(nb).cpu().numpy().reshape((d,) * (2 * k))
+        pos = {site: p for p, site in enumerate(kept)}
+        perm = [2 * pos[i] for i in node_indices] + [2 * pos[i] + 1 for i in node_indices]
+        return np.ascontiguousarray(vals.transpose(perm)).reshape(d ** k, d ** k)
+
+    def site_marginals(self) -> np.ndarray:
+        """(nqudits, d) float32: the diagonal of every single-site reduced
+        density matrix (not normalised), from one device pass."""
+        if not self.is_valid():
+            raise ValueError("MPS is invalid.")
+        d, n = self._qudit_dimension, self._nqudits
+        chis = _int_array(self._chis())
+        lib = self._lib()
+        ws = _WS.get(self._device, lib.mps_marginals_workspace_bytes(chis, n, d), "marg")
+        out = np.zeros((n, d), dtype=np.float32)
+        _native.check(lib.mps_site_marginals(
+            self._stream(), _ptr_array(self._sites), chis, n, d, ctypes.c_void_p(ws.data_ptr()),
+            ws.numel(), out.ctypes.data_as(ctypes.c_void_p)))
+        return out
 
     def sample(self, nsamples: int, as_hist: bool = False, as_string: bool = False):
-        raise NotImplementedError("sampling is outside this build's scope")
+        """Samples as MPS.sample does (core.py:669-709): each site's digit is
+        drawn with np.random.choice from that site's marginal,
+        reduced_density_matrix(i).diagonal().real (core.py:655-667), in the
+        same order of NumPy global-RNG calls, so a seeded np.random gives the
+        reference's draws; the marginals come from one device pass."""
+        if not isinstance(nsamples, int):
+            raise ValueError(f"Arg nsamples should be an int but is a {type(nsamples)}.")
+        if nsamples <= 0:
+            raise ValueError(f"Arg nsamples should be positive but is {nsamples}.")
+        if as_hist:
+            as_string = True
+        probs = self.site_marginals()
+        states = list(range(self._qudit_dimension))
+        raw = []
+        for _ in range(nsamples):
+            string = [np.random.choice(states, size=1, p=probs[i])[0]
+                      for i in range(self._nqudits)]
+            raw.append("".join(str(bit) for bit in string) if as_string else string)
+        if as_hist:
+            hist = {}
+            for bitstring in raw:
+                hist[bitstring] = hist.get(bitstring, 0) + 1
+            return hist
+        return raw
 
     @staticmethod
-    def from_wavefunction(wavefunction, nqudits, qudit_dimension=2, tensor_prefix="q"):
-        raise NotImplementedError("from_wavefunction is outside this build's scope")
+    def from_wavefunction(wavefunction, nqudits: int, qudit_dimension: int = 2,
+                          tensor_prefix: str = "q") -> "MPS":
+        """MPS of a state vector by successive SVDs across every cut, all
+        singular values kept (core.py:245-328).  The state is the reference's;
+        the gauge is left-canonical (U on each site, S V^H carried right)
+        where TensorNetwork's split_node puts sqrt(S) on both sides.  Every
+        split runs through the Jacobi SVD kernel, so d^(nqudits-1) must not
+        exceed its 1792-row limit (11 qubits, 7 qutrits)."""
+        if not isinstance(wavefunction, (list, tuple, np.ndarray)):
+            raise TypeError("Invalid type for wavefunction.")
+        wavefunction = np.array(wavefunction)
+        if len(wavefunction.shape) != 1:
+            raise ValueError("Invalid shape for wavefunction. Should be a vector.")
+        if nqudits < 2:
+            raise ValueError("At least two qudits are required.")
+        d = int(qudit_dimension)
+        if wavefunction.size != d ** nqudits:
+            raise ValueError(
+                "Mismatch between wavefunction, qudit_dimension, and nqudits. "
+                f"Expected {d ** nqudits} elements in the wavefunction, but wavefunction has "
+                f"{wavefunction.size} elements.")
+        mps = MPS(nqudits, d, tensor_prefix)
+        dev, stream = mps._device, mps._stream()
+        rest = torch.from_numpy(np.ascontiguousarray(wavefunction.astype(np.complex64))).to(dev)
+        chi = 1
+        sites = []
+        for i in range(nqudits - 1):
+            left, right, _ = _given_svd(dev, stream, rest.view(chi * d, d ** (nqudits - 1 - i)),
+                                        True)
+            k = int(left.shape[1])
+            sites.append(left.reshape(chi, d, k))
+            rest = right
+            chi = k
+        sites.append(rest.reshape(chi, d, 1))
+        mps._sites = sites
+        return mps
 
-    def orthonormalize_right_edge_of(self, node_index: int, threshold: float = 1e-8):
-        raise NotImplementedError("orthonormalization is outside this build's scope")
+    def orthonormalize_right_edge_of(self, node_index: int, threshold: float = 1e-8) -> None:
+        """SVD of site i with rows (left bond, digit): site i <- U, site i+1
+        <- S V^H . site i+1, dropping the smallest values whose tail norm is
+        <= threshold * norm (core.py:847-891)."""
+        if not 0 <= node_index < self._nqudits - 1:
+            raise ValueError("Invalid edge index.")
+        i = node_index
+        node = self._sites[i]
+        cl, d, cr = (int(x) for x in node.shape)
+        max_err = threshold * self.norm()
+        left, right, s = _given_svd(self._device, self._stream(), node.reshape(cl * d, cr), True)
+        keep = kept_by_truncation_error(s, max_err)
+        r = int(left.shape[1])
+        nxt = self._sites[i + 1]
+        c2 = int(nxt.shape[2])
+        new_next = torch.empty((keep, d, c2), dtype=torch.complex64, device=self._device)
+        _cgemm(self._lib(), self._stream(), keep, d * c2, cr, right, 0, cr, 1, 0,
+               nxt, 0, d * c2, 1, 0, new_next, 0, d * c2, 1)
+        self._sites[i] = left[:, :keep].reshape(cl, d, keep) if keep == r else \
+            left[:, :keep].contiguous().reshape(cl, d, keep)
+        self._sites[i + 1] = new_next
 
-    def orthonormalize_left_edge_of(self, node_index: int, threshold: float = 1e-8):
-        raise NotImplementedError("orthonormalization is outside this build's scope")
+    def orthonormalize_left_edge_of(self, node_index: int, threshold: float = 1e-8) -> None:
+        """SVD of site i with columns (digit, right bond): site i <- V^H,
+        site i-1 <- site i-1 . U S, dropping the smallest values whose tail
+        norm is <= threshold * norm (core.py:893-937)."""
+        if not 0 < node_index <= self._nqudits - 1:
+            raise ValueError("Invalid edge index.")
+        i = node_index
+        node = self._sites[i]
+        cl, d, cr = (int(x) for x in node.shape)
+        max_err = threshold * self.norm()
+        left, right, s = _given_svd(self._device, self._stream(), node.reshape(cl, d * cr), False)
+        keep = kept_by_truncation_error(s, max_err)
+        r = int(left.shape[1])
+        prev = self._sites[i - 1]
+        c0 = int(prev.shape[0])
+        new_prev = torch.empty((c0, d, keep), dtype=torch.complex64, device=self._device)
+        _cgemm(self._lib(), self._stream(), c0 * d, keep, cl, prev, 0, cl, 1, 0,
+               left, 0, r, 1, 0, new_prev, 0, keep, 1)
+        self._sites[i] = right[:keep].reshape(keep, d, cr)
+        self._sites[i - 1] = new_prev
 
     # -- one-qudit gates ---------------------------------------------------
     def _check_one_qudit(self, gate, node_index):
@@ -466,16 +689,21 @@ class MPS:
         unitary = is_unitary(np.asarray(mat))
         renorm = kwargs.get("renormalize_after_non_unitary") is not False
         ortho = kwargs.get("ortho_after_non_unitary") is not False
-        if not unitary and ortho:
-            raise NotImplementedError(
-                "non-unitary one-qudit gates with ortho_after_non_unitary=True are outside "
-                "this build's scope; pass ortho_after_non_unitary=False")
         norm = self.norm() if (not unitary and renorm) else None
         site = self._sites[node_index]
         g = self._to_device_gate(mat)
         _native.check(self._lib().mps_apply_1q(
             self._stream(), ctypes.c_void_p(site.data_ptr()), int(site.shape[0]),
             self._qudit_dimension, int(site.shape[2]), ctypes.c_void_p(g.data_ptr())))
+        if not unitary and ortho:
+            # core.py:828-842
+            if node_index == 0:
+                self.orthonormalize_right_edge_of(node_index)
+            elif node_index == self._nqudits - 1:
+                self.orthonormalize_left_edge_of(node_index)
+            else:
+                self.orthonormalize_right_edge_of(node_index)
+                self.orthonormalize_left_edge_of(node_index)
         if norm is not None:
             self.renormalize(norm)
 

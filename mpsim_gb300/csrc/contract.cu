@@ -1,11 +1,14 @@
 // One-qudit gate, left-to-right contraction sweeps (overlap/norm,
-// wavefunction, sampled amplitudes) and elementwise scale/conjugate.
+// wavefunction, sampled amplitudes, single-site marginals), a strided batched
+// complex GEMM and elementwise scale/conjugate.
 //
 // mpsim performs these with TensorNetwork contractions on the host:
 //   apply_one_qudit_gate   mpsim/core.py:820-826
 //   wavefunction           mpsim/core.py:483-500
 //   inner_product / norm   mpsim/core.py:543-565
 //   renormalize / dagger   mpsim/core.py:567-594, 502-505
+//   marginals for sample   mpsim/core.py:655-667 (reduced_density_matrix(i)
+//                          diagonal, core.py:596-653)
 #include <atomic>
 #include <string>
 
@@ -107,8 +110,10 @@ __global__ void scale_kernel(cf* __restrict__ x, size_t count, cf alpha, int con
 
 // ---------------------------------------------------------------------------
 // Generic complex GEMM C = op(A) op(B) with arbitrary element strides and
-// optional conjugation.  64x64 tile, K chunks of 16, 256 threads, each thread
-// 4x4 outputs at (ty + 16i, tx + 16j).
+// optional conjugation, batched over blockIdx.z with element strides bsa,
+// bsb, bsc between batches (zero: the same matrix for every batch).  64x64
+// tile, K chunks of 16, 256 threads, each thread 4x4 outputs at
+// (ty + 16i, tx + 16j).
 struct GemmArgs {
     int M, N, K;
     const cf* A;
@@ -119,11 +124,16 @@ struct GemmArgs {
     int conjB;
     cf* C;
     long long scm, scn;
+    int batch;                  // 0 or 1: one product
+    long long bsa, bsb, bsc;
 };
 
 __global__ void __launch_bounds__(256) cgemm_kernel(GemmArgs g) {
     __shared__ cf As[16][64];
     __shared__ cf Bs[16][64];
+    g.A += blockIdx.z * g.bsa;
+    g.B += blockIdx.z * g.bsb;
+    g.C += blockIdx.z * g.bsc;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
     cf acc[4][4];
@@ -185,9 +195,10 @@ __global__ void __launch_bounds__(256) cgemm_kernel(GemmArgs g) {
 }
 
 int cgemm(const GemmArgs& a, cudaStream_t s) {
-    if (a.M <= 0 || a.N <= 0) return MPS_OK;
-    dim3 grid((a.N + 63) / 64, (a.M + 63) / 64);
+    if (a.M <= 0 || a.N <= 0 || a.batch < 0) return MPS_OK;
+    dim3 grid((a.N + 63) / 64, (a.M + 63) / 64, a.batch > 1 ? a.batch : 1);
     if (grid.y > 65535) return fail(MPS_ERR_ARG, "cgemm: too many rows");
+    if (grid.z > 65535) return fail(MPS_ERR_ARG, "cgemm: batch above 65535");
     cgemm_kernel<<<grid, 256, 0, s>>>(a);
     MPS_LAUNCH_CHECK("cgemm_kernel");
     return MPS_OK;
@@ -204,6 +215,29 @@ __global__ void select_kernel(const cf* __restrict__ full, cf* __restrict__ env,
         env[t] = (x >= 0 && x < d) ? full[sidx * (size_t)d * chir + (size_t)x * chir + r]
                                    : cmake(0.f, 0.f);
     }
+}
+
+// probs[x] = Re sum_{l, r} conj(A[l, x, r]) W[l, x, r]: block x, FP64 sum.
+__global__ void __launch_bounds__(256) marginal_kernel(const cf* __restrict__ A,
+                                                       const cf* __restrict__ W, int chil,
+                                                       int d, int chir, float* __restrict__ probs) {
+    __shared__ double part[256];
+    const int x = blockIdx.x;
+    const size_t total = (size_t)chil * chir;
+    double acc = 0.0;
+    for (size_t t = threadIdx.x; t < total; t += blockDim.x) {
+        const size_t l = t / chir, r = t % chir;
+        const size_t o = (l * d + x) * chir + r;
+        const cf a = A[o], w = W[o];
+        acc += (double)a.x * w.x + (double)a.y * w.y;
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) probs[x] = (float)part[0];
 }
 
 __global__ void fill_one_kernel(cf* x, size_t count) {
@@ -404,5 +438,108 @@ extern "C" int mps_amplitudes(void* stream, const mps_c64* const* sites, const i
         MPS_LAUNCH_CHECK("select_kernel");
         cur ^= 1;
     }
+    return MPS_OK;
+}
+
+extern "C" int mps_cgemm(void* stream, int m, int n, int k, const mps_c64* a, long long sam,
+                         long long sak, int conj_a, const mps_c64* b, long long sbk,
+                         long long sbn, int conj_b, mps_c64* c, long long scm, long long scn,
+                         int batch, long long bsa, long long bsb, long long bsc) {
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (m < 0 || n < 0 || k < 0 || batch < 0 || (m > 0 && n > 0 && (!c || (k > 0 && (!a || !b)))))
+        return fail(MPS_ERR_ARG, "mps_cgemm: bad arguments");
+    GemmArgs g{m, n, k, reinterpret_cast<const cf*>(a), sam, sak, conj_a ? 1 : 0,
+               reinterpret_cast<const cf*>(b), sbk, sbn, conj_b ? 1 : 0,
+               reinterpret_cast<cf*>(c), scm, scn, batch, bsa, bsb, bsc};
+    return cgemm(g, s);
+}
+
+extern "C" size_t mps_marginals_workspace_bytes(const int* chis, int n, int d) {
+    if (!chis || n < 1 || d < 1) return 0;
+    size_t envs = 0, maxchi = 1;
+    for (int i = 0; i < n; ++i) envs += (size_t)chis[i] * chis[i];
+    for (int i = 0; i <= n; ++i) maxchi = max(maxchi, (size_t)chis[i]);
+    const size_t cells = envs + 2 * maxchi * maxchi + 2 * maxchi * d * maxchi;
+    return align_up(cells * sizeof(cf) + (size_t)n * d * sizeof(float) + 1024, 256);
+}
+
+extern "C" int mps_site_marginals(void* stream, const mps_c64* const* sites, const int* chis,
+                                  int n, int d, void* workspace, size_t workspace_bytes,
+                                  float* probs_host) {
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (n < 1 || d < 1 || !sites || !chis || !probs_host)
+        return fail(MPS_ERR_ARG, "mps_site_marginals: bad arguments");
+    if (chis[0] != 1 || chis[n] != 1) return fail(MPS_ERR_ARG, "mps_site_marginals: end bonds must be 1");
+    if (!workspace || workspace_bytes < mps_marginals_workspace_bytes(chis, n, d))
+        return fail(MPS_ERR_WORKSPACE, "mps_site_marginals: workspace too small");
+    size_t maxchi = 1;
+    for (int i = 0; i <= n; ++i) maxchi = max(maxchi, (size_t)chis[i]);
+    // left environments L_i (ket, bra), i = 0..n-1, packed
+    cf* base = static_cast<cf*>(workspace);
+    size_t off = 0;
+    cf* R[2];
+    cf* U;
+    cf* W;
+    {
+        size_t envs = 0;
+        for (int i = 0; i < n; ++i) envs += (size_t)chis[i] * chis[i];
+        R[0] = base + envs;
+        R[1] = R[0] + maxchi * maxchi;
+        U = R[1] + maxchi * maxchi;
+        W = U + maxchi * d * maxchi;
+    }
+    float* probs_dev = reinterpret_cast<float*>(W + maxchi * d * maxchi);
+    fill_one_kernel<<<1, 32, 0, s>>>(base, 1);
+    MPS_LAUNCH_CHECK("fill_one_kernel");
+    for (int i = 0; i + 1 < n; ++i) {
+        const int cl = chis[i], cr = chis[i + 1];
+        const cf* A = reinterpret_cast<const cf*>(sites[i]);
+        cf* L = base + off;
+        cf* Ln = L + (size_t)cl * cl;
+        // U[l, (x, r')] = sum_l' L[l, l'] conj(A[l', x, r'])
+        GemmArgs g1{cl, d * cr, cl, L, cl, 1, 0, A, (long long)d * cr, 1, 1, U, (long long)d * cr, 1};
+        int rc = cgemm(g1, s);
+        if (rc) return rc;
+        // L'[r, r'] = sum_(l,x) A[(l,x), r] U[(l,x), r']
+        if (cr > 0 && cl == 0) {
+            MPS_CUDA_CHECK(cudaMemsetAsync(Ln, 0, (size_t)cr * cr * sizeof(cf), s));
+        } else {
+            GemmArgs g2{cr, cr, cl * d, A, 1, cr, 0, U, cr, 1, 0, Ln, cr, 1};
+            rc = cgemm(g2, s);
+            if (rc) return rc;
+        }
+        off += (size_t)cl * cl;
+    }
+    // right-to-left: p_i(x) = sum L_i[l,l'] A[l,x,r] conj(A[l',x,r']) R_i[r,r']
+    fill_one_kernel<<<1, 32, 0, s>>>(R[0], 1);
+    MPS_LAUNCH_CHECK("fill_one_kernel");
+    int cur = 0;
+    for (int i = n - 1; i >= 0; --i) {
+        const int cl = chis[i], cr = chis[i + 1];
+        const cf* A = reinterpret_cast<const cf*>(sites[i]);
+        cf* L = base + off;
+        // U[(l, x), r'] = sum_r A[(l, x), r] R[r, r']
+        GemmArgs g1{cl * d, cr, cr, A, cr, 1, 0, R[cur], cr, 1, 0, U, cr, 1};
+        int rc = cgemm(g1, s);
+        if (rc) return rc;
+        // W[l', (x, r')] = sum_l L[l, l'] U[l, (x, r')]
+        GemmArgs g2{cl, d * cr, cl, L, 1, cl, 0, U, (long long)d * cr, 1, 0, W, (long long)d * cr, 1};
+        rc = cgemm(g2, s);
+        if (rc) return rc;
+        marginal_kernel<<<d, 256, 0, s>>>(A, W, cl, d, cr, probs_dev + (size_t)i * d);
+        MPS_LAUNCH_CHECK("marginal_kernel");
+        if (i > 0) {
+            // R'[l, l'] = sum_(x, r') U[l, (x, r')] conj(A[l', (x, r')])
+            GemmArgs g3{cl, cl, d * cr, U, (long long)d * cr, 1, 0, A, 1, (long long)d * cr, 1,
+                        R[cur ^ 1], cl, 1};
+            rc = cgemm(g3, s);
+            if (rc) return rc;
+            cur ^= 1;
+            off -= (size_t)chis[i - 1] * chis[i - 1];
+        }
+    }
+    MPS_CUDA_CHECK(cudaMemcpyAsync(probs_host, probs_dev, (size_t)n * d * sizeof(float),
+                                   cudaMemcpyDeviceToHost, s));
+    MPS_CUDA_CHECK(cudaStreamSynchronize(s));
     return MPS_OK;
 }

@@ -9,6 +9,11 @@
 // entries the gate needs for the same theta tile -- then mixes the tile with
 // the gate in shared memory and writes theta straight into the Jacobi working
 // matrix X (column-major; conjugate-transposed for wide theta).
+//
+// A job flagged MPS_JOB_THETA_GIVEN carries theta itself: a points to the
+// (chi_l*d) x (d*chi_r) matrix, row-major, and the same CTAs copy their tile
+// of it into X (the plain truncated SVD of a given matrix, which
+// from_wavefunction and the orthonormalisation of one site use).
 #include "twoq.cuh"
 
 namespace mps {
@@ -30,6 +35,7 @@ merge_gate_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
     if (l0 >= chil || r0 >= chir) return;
     const int m = chil * d, n = d * chir;
     const bool tall = m >= n;
+    const bool given = (job.flags & MPS_JOB_THETA_GIVEN) != 0;   // block-uniform
 
     __shared__ union {
         struct { cf a[KC][TILE]; cf b[KC][TILE]; } ld;
@@ -47,7 +53,7 @@ merge_gate_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
     const cf* A = reinterpret_cast<const cf*>(job.a);
     const cf* B = reinterpret_cast<const cf*>(job.b);
     const int row0 = l0 * d;
-    for (int k0 = 0; k0 < chim; k0 += KC) {
+    for (int k0 = 0; k0 < (given ? 0 : chim); k0 += KC) {
 #pragma unroll
         for (int q = 0; q < (KC * TILE) / NT; ++q) {
             const int idx = tid + q * NT;
@@ -99,15 +105,19 @@ merge_gate_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
         const int l = l0 + tr / d, ap = tr % d;
         const int bp = tc / TR, rr = tc % TR, r = r0 + rr;
         if (l >= chil || r >= chir) continue;
-        const cf* grow = G + (size_t)(ap * d + bp) * dd;
-        const int rbase = tr - ap;                // tile row of (l, a=0)
-        cf th = cmake(0.f, 0.f);
-        for (int a = 0; a < d; ++a)
-            for (int b = 0; b < d; ++b)
-                cfma(th, __ldg(reinterpret_cast<const float2*>(grow + a * d + b)),
-                     sh.mt[rbase + a][b * TR + rr]);
         const int trow = l * d + ap;              // theta row
         const int tcol = bp * chir + r;           // theta column
+        cf th = cmake(0.f, 0.f);
+        if (given) {
+            th = A[(size_t)trow * n + tcol];
+        } else {
+            const cf* grow = G + (size_t)(ap * d + bp) * dd;
+            const int rbase = tr - ap;            // tile row of (l, a=0)
+            for (int a = 0; a < d; ++a)
+                for (int b = 0; b < d; ++b)
+                    cfma(th, __ldg(reinterpret_cast<const float2*>(grow + a * d + b)),
+                         sh.mt[rbase + a][b * TR + rr]);
+        }
         if (tall) {
             X[(size_t)tcol * g.lslot + trow] = th;
             if (!track_v) T[(size_t)tcol * g.lslot + trow] = th;

@@ -21,6 +21,17 @@ computes through TensorNetwork 0.2.1 and LAPACK:
 * ``wavefunction``                  mpsim/core.py:483-500 (big-endian).
 * ``inner_product`` / ``norm``      mpsim/core.py:507-565 (conj on *other*).
 * ``renormalize``                   mpsim/core.py:567-594.
+* ``reduced_density_matrix``        mpsim/core.py:596-653 (ket digits of the
+                                     kept sites in the given order, then bra).
+* ``site_marginals`` / ``sample``   mpsim/core.py:655-709 (each digit drawn
+                                     from that site's marginal of the
+                                     unconditioned state).
+* ``from_wavefunction``             mpsim/core.py:245-328 (split_node at every
+                                     cut, nothing truncated, sqrt(S) on both
+                                     sides).
+* ``orthonormalize_*_edge_of``      mpsim/core.py:847-937 (split_node_full_svd
+                                     with max_truncation_err = threshold*norm).
+* non-unitary one-qudit gates       mpsim/core.py:793-845.
 * ``haar_random_unitary``           mpsim/gates.py:248-286 (Mezzadri QR).
 
 Site tensors are stored as (chi_left, d, chi_right) arrays.  The reference
@@ -99,11 +110,82 @@ class OracleMPS:
         return new
 
     # -- gates -------------------------------------------------------------
-    def apply_one_qudit_gate(self, gate, i):
+    def apply_one_qudit_gate(self, gate, i, renormalize_after_non_unitary=True,
+                             ortho_after_non_unitary=True):
         u = np.asarray(gate).astype(self.dtype)
+        unitary = bool(np.allclose(u.conj().T @ u, np.identity(u.shape[0]), atol=1e-5))
+        norm = self.norm() if (not unitary and renormalize_after_non_unitary) else None
         s = self.sites[i]
         # new[l, a', r] = sum_a U[a', a] s[l, a, r]   (core.py:820-826)
         self.sites[i] = np.einsum("xa,lar->lxr", u, s).astype(self.dtype)
+        if not unitary and ortho_after_non_unitary:   # core.py:828-842
+            if i == 0:
+                self.orthonormalize_right_edge_of(i)
+            elif i == self.n - 1:
+                self.orthonormalize_left_edge_of(i)
+            else:
+                self.orthonormalize_right_edge_of(i)
+                self.orthonormalize_left_edge_of(i)
+        if norm is not None:                          # core.py:844-845
+            self.renormalize(norm)
+
+    @staticmethod
+    def _kept_by_error(s, max_err):
+        """split_node_full_svd's max_truncation_err rule (TensorNetwork
+        0.2.1): count of sqrt(cumsum(s[::-1]^2)) above the bound."""
+        errs = np.sqrt(np.cumsum(np.square(s[::-1])))
+        return int(np.count_nonzero(errs > max_err))
+
+    def orthonormalize_right_edge_of(self, i, threshold=1e-8):
+        """core.py:847-891: SVD with rows (digit, left bond), site <- U,
+        right neighbour <- S V^H . neighbour."""
+        if not 0 <= i < self.n - 1:
+            raise ValueError("Invalid edge index.")
+        a = self.sites[i]
+        chil, d, chir = a.shape
+        max_err = threshold * self.norm()
+        u, s, vh = np.linalg.svd(a.reshape(chil * d, chir), full_matrices=False)
+        k = self._kept_by_error(s, max_err)
+        right = (s[:k].astype(self.dtype)[:, None] * vh[:k]).astype(self.dtype)
+        nxt = self.sites[i + 1]
+        self.sites[i] = np.ascontiguousarray(u[:, :k].reshape(chil, d, k))
+        self.sites[i + 1] = (right @ nxt.reshape(chir, -1)).reshape(k, d, nxt.shape[2])
+
+    def orthonormalize_left_edge_of(self, i, threshold=1e-8):
+        """core.py:893-937: SVD with columns (digit, right bond), site <-
+        V^H, left neighbour <- neighbour . U S."""
+        if not 0 < i <= self.n - 1:
+            raise ValueError("Invalid edge index.")
+        a = self.sites[i]
+        chil, d, chir = a.shape
+        max_err = threshold * self.norm()
+        u, s, vh = np.linalg.svd(a.reshape(chil, d * chir), full_matrices=False)
+        k = self._kept_by_error(s, max_err)
+        left = (u[:, :k] * s[:k].astype(self.dtype)[None, :]).astype(self.dtype)
+        prev = self.sites[i - 1]
+        self.sites[i] = np.ascontiguousarray(vh[:k].reshape(k, d, chir))
+        self.sites[i - 1] = (prev.reshape(-1, chil) @ left).reshape(prev.shape[0], d, k)
+
+    @staticmethod
+    def from_wavefunction(psi, nqudits, qudit_dimension=2, dtype=np.complex64):
+        """core.py:245-328: split at every cut with TensorNetwork's
+        split_node (full SVD, nothing truncated, sqrt(S) on both sides)."""
+        d = qudit_dimension
+        o = OracleMPS(nqudits, d, dtype)
+        rest = np.asarray(psi).astype(o.dtype).reshape(1, -1)
+        chi = 1
+        sites = []
+        for i in range(nqudits - 1):
+            mat = rest.reshape(chi * d, -1)
+            u, s, vh = np.linalg.svd(mat, full_matrices=False)
+            sq = np.sqrt(s).astype(o.dtype)
+            k = s.size
+            sites.append((u * sq[None, :]).reshape(chi, d, k))
+            rest = sq[:, None] * vh
+            chi = k
+        sites.append(rest.reshape(chi, d, 1))
+        o.sites = [np.ascontiguousarray(t) for t in sites]
+        return o
 
     def apply_two_qudit_gate(self, gate, i, j, **kwargs):
         g = np.asarray(gate).astype(self.dtype).reshape((self.d,) * 4)
@@ -215,6 +297,55 @@ class OracleMPS:
             raise ValueError("Norm of MPS is numerically zero, cannot renormalize.")
         factor = (to_norm / norm) ** (1 / self.n)
         self.sites = [(factor * s).astype(self.dtype) for s in self.sites]
+
+    def reduced_density_matrix(self, node_indices):
+        """core.py:596-653: rho[(ket digits of node_indices in the given
+        order), (bra digits)], the other sites traced out, not normalised."""
+        try:
+            node_indices = tuple(iter(node_indices))
+        except TypeError:
+            node_indices = (node_indices,)
+        kept = sorted(node_indices)
+        d = self.d
+        # env[b, l, l'] with b = (a_1, a_1', a_2, a_2', ...) over kept sites
+        env = np.ones((1, 1, 1), dtype=self.dtype)
+        for i, s in enumerate(self.sites):
+            f = np.einsum("bkl,kar->blar", env, s)            # b, l', a, r
+            if i in kept:
+                env = np.einsum("blar,lcs->bacrs", f, np.conj(s))
+                env = env.reshape(-1, s.shape[2], s.shape[2])
+            else:
+                env = np.einsum("blar,las->brs", f, np.conj(s))
+        k = len(kept)
+        vals = env.reshape((d,) * (2 * k))
+        pos = {site: p for p, site in enumerate(kept)}
+        perm = [2 * pos[i] for i in node_indices] + [2 * pos[i] + 1 for i in node_indices]
+        return np.ascontiguousarray(vals.transpose(perm)).reshape(d ** k, d ** k)
+
+    def site_marginals(self):
+        """reduced_density_matrix(i).diagonal().real for every site
+        (core.py:661), as float of the state's precision."""
+        real = np.float32 if self.dtype == np.complex64 else np.float64
+        return np.stack([self.reduced_density_matrix(i).diagonal().real.astype(real)
+                         for i in range(self.n)])
+
+    def sample(self, nsamples, as_hist=False, as_string=False):
+        """core.py:655-709: per sample and site, np.random.choice over the
+        digits with that site's marginal (global NumPy RNG)."""
+        if as_hist:
+            as_string = True
+        probs = self.site_marginals()
+        states = list(range(self.d))
+        raw = []
+        for _ in range(nsamples):
+            string = [np.random.choice(states, size=1, p=probs[i])[0] for i in range(self.n)]
+            raw.append("".join(str(b) for b in string) if as_string else string)
+        if as_hist:
+            hist = {}
+            for b in raw:
+                hist[b] = hist.get(b, 0) + 1
+            return hist
+        return raw
 
     def amplitudes(self, bitstrings):
         """<x|psi> for each row x of ``bitstrings`` (shape (S, n))."""

@@ -22,6 +22,10 @@ What it does:
 5. For the 64-qubit workload, which the reference's per-gate norm sweep makes
    too slow to run through the reference, stores the oracle's results
    (complex64 and complex128) only.
+6. ``observables.npz``: reduced density matrices, single-site marginals,
+   seeded samples, ``from_wavefunction``, ``orthonormalize_*_edge_of``,
+   non-unitary one-qudit gates and expectation values, all from the
+   reference's own ``MPS`` on small seeded states (complex64).
 """
 
 from __future__ import annotations
@@ -257,6 +261,92 @@ def known_answer_fixture(core, tn):
     print("known answers:", ", ".join(cases))
 
 
+# Small seeded states for the observables fixture: (name, nqudits, d, depth,
+# maxsvals, seed).  The GPU tests rebuild them from the same circuits.
+OBS_STATES = [("q6", 6, 2, 3, None, 21), ("t4", 4, 3, 2, None, 22), ("q8trunc", 8, 2, 5, 3, 23)]
+OBS_RDM = {"q6": [(0,), (3,), (1, 2), (4, 1), (0, 5, 2)], "t4": [(1,), (0, 3), (2, 1)],
+           "q8trunc": [(2,), (5, 6)]}
+
+
+def observables_fixture(core, tn):
+    """Row (f) functions of the reference, run through the reference."""
+    from mpsim import gates as G
+    out = {}
+
+    def build(n, d, depth, maxsvals, seed):
+        circ = C.brickwork(n, depth, d=d, maxsvals=maxsvals, seed=seed)
+        m = core.MPS(n, d)
+        kw = {} if maxsvals is None else {"maxsvals": maxsvals}
+        for kind, sites, mat in circ.operations():
+            g = np.asarray(mat).astype(np.complex64)
+            if kind == 1:
+                m.apply_one_qudit_gate(tn.Node(g), sites[0])
+            else:
+                m.apply_two_qudit_gate(tn.Node(g.reshape((d,) * 4)), sites[0], sites[1], **kw)
+        return m
+
+    states = {}
+    for name, n, d, depth, maxs, seed in OBS_STATES:
+        m = build(n, d, depth, maxs, seed)
+        states[name] = m
+        out[f"{name}_wf"] = m.wavefunction()
+        for idx in OBS_RDM[name]:
+            key = "_".join(str(i) for i in idx)
+            out[f"{name}_rdm_{key}"] = m.reduced_density_matrix(list(idx))
+        out[f"{name}_marginals"] = np.stack(
+            [m.reduced_density_matrix(i).diagonal().real for i in range(n)])
+    # seeded samples (the normalised states only: a truncated state's
+    # marginals do not sum to one and np.random.choice refuses them)
+    np.random.seed(7)
+    out["q6_samples"] = np.asarray(states["q6"].sample(25), dtype=np.int64)
+    np.random.seed(8)
+    hist = states["q6"].sample(40, as_hist=True)
+    out["q6_hist_keys"] = np.asarray(sorted(hist))
+    out["q6_hist_counts"] = np.asarray([hist[k] for k in sorted(hist)], dtype=np.int64)
+    np.random.seed(9)
+    out["t4_samples"] = np.asarray(states["t4"].sample(20, as_string=True))
+    # from_wavefunction
+    rng = np.random.default_rng(31)
+    for name, n, d in (("fw_q6", 6, 2), ("fw_t4", 4, 3)):
+        psi = (rng.normal(size=d ** n) + 1j * rng.normal(size=d ** n)).astype(np.complex64)
+        psi /= np.linalg.norm(psi)
+        m = core.MPS.from_wavefunction(psi, n, d)
+        out[f"{name}_psi"] = psi
+        out[f"{name}_wf"] = m.wavefunction()
+        out[f"{name}_bonds"] = np.asarray(m.bond_dimensions())
+    # orthonormalisation of one edge
+    m = build(6, 2, 3, None, 21)
+    m.orthonormalize_right_edge_of(2)
+    out["ortho_r2_wf"], out["ortho_r2_bonds"] = m.wavefunction(), np.asarray(m.bond_dimensions())
+    m.orthonormalize_left_edge_of(4)
+    out["ortho_l4_wf"], out["ortho_l4_bonds"] = m.wavefunction(), np.asarray(m.bond_dimensions())
+    # non-unitary gates: a projector on a GHZ state (exact zero singular
+    # values: orthonormalisation must cut the bonds to 1), and a general
+    # non-unitary gate with each keyword combination
+    m = core.MPS(4)
+    m.h(0)
+    for i in range(3):
+        m.cnot(i, i + 1)
+    m.apply_one_qudit_gate(G.computational_basis_projector(0), 1)
+    out["ghz_proj_wf"], out["ghz_proj_bonds"] = m.wavefunction(), np.asarray(m.bond_dimensions())
+    damp = np.array([[1.0, 0.0], [0.0, 0.4]], dtype=np.complex64)
+    for tag, kw in (("default", {}), ("noortho", {"ortho_after_non_unitary": False}),
+                    ("norenorm", {"renormalize_after_non_unitary": False}), ("end", {})):
+        m = build(6, 2, 3, None, 21)
+        site = 5 if tag == "end" else 3
+        m.apply_one_qudit_gate(tn.Node(damp), site, **kw)
+        out[f"nonunit_{tag}_wf"] = m.wavefunction()
+        out[f"nonunit_{tag}_bonds"] = np.asarray(m.bond_dimensions())
+        out[f"nonunit_{tag}_norm"] = np.float64(m.norm())
+    # expectation values
+    m = states["q6"]
+    out["expect_z1"] = np.float64(m.expectation(core.MPSOperation(G.zgate(), 1)))
+    out["expect_x4"] = np.float64(m.expectation(core.MPSOperation(G.xgate(), 4)))
+    out["expect_cnot23"] = np.float64(m.expectation(core.MPSOperation(G.cnot(), (2, 3))))
+    np.savez_compressed(os.path.join(HERE, "observables.npz"), **out)
+    print("observables:", len(out), "arrays")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -278,6 +368,8 @@ def main():
     if only in (None, "cfg1"):
         golden_reference_circuit(core, tn, "brickwork_48q_d24_chi128",
                                  C.workload("brickwork_48q_d24_chi128"), 64)
+    if only in (None, "obs"):
+        observables_fixture(core, tn)
     if only in (None, "cfg2"):
         golden_oracle_circuit("brickwork_64q_d40_chi256",
                               C.workload("brickwork_64q_d40_chi256"), 64)
