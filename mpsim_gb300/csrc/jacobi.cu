@@ -1094,6 +1094,106 @@ complete_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
 }
 
 // ---------------------------------------------------------------------------
+// Exact power-of-two scaling of every job's theta to a Frobenius norm in
+// [1, 2) before the SVD, undone on the outputs afterwards.  A state whose norm
+// has decayed through truncation (to 1e-9 at the end of a 64-qubit, depth-40,
+// maxsvals=256 circuit) gives squared column norms near 1e-19 and |gamma|^2
+// below the smallest normal float, where FP32 keeps only a few bits; LAPACK,
+// which the reference uses, scales for the same reason.  Multiplying by a
+// power of two changes no bit of the relative arithmetic.
+
+__global__ void __launch_bounds__(256) theta_norm_kernel(TwoQGeom g) {
+    __shared__ double part[256];
+    const int j = blockIdx.y;
+    const size_t count = (size_t)g.lslot * g.cslot;
+    const cf* X = g.X + (size_t)j * count;
+    double acc = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const cf x = X[t];
+        acc += (double)x.x * x.x + (double)x.y * x.y;
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(g.nrm2 + j, part[0]);
+}
+
+__device__ __forceinline__ int theta_scale_exponent(double n2) {
+    if (!(n2 > 0.0) || !isfinite(n2)) return 0;       // zero or NaN/Inf: leave as is
+    int ex;
+    frexp(sqrt(n2), &ex);                             // |theta| = f 2^ex, f in [0.5, 1)
+    int e = 1 - ex;
+    return e < -120 ? -120 : (e > 120 ? 120 : e);
+}
+
+__global__ void __launch_bounds__(256) theta_scale_kernel(const mps_2q_job* __restrict__ jobs,
+                                                          TwoQGeom g) {
+    const int j = blockIdx.y;
+    const int e = theta_scale_exponent(g.nrm2[j]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) g.scale[j] = e;
+    if (e == 0) return;
+    const float f = ldexpf(1.f, e);
+    const size_t count = (size_t)g.lslot * g.cslot;
+    cf* X = g.X + (size_t)j * count;
+    const mps_2q_job job = jobs[j];
+    cf* T = job_tracks_v(job.chi_l * g.d, g.d * job.chi_r, job.keep_left_canonical)
+                ? nullptr : g.T + (size_t)j * count;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count;
+         t += (size_t)gridDim.x * blockDim.x) {
+        X[t] = cscale(X[t], f);
+        if (T) T[t] = cscale(T[t], f);
+    }
+}
+
+// The singular values, the discarded weight and the site that carries S
+// (the right one for keep_left_canonical, else the left) back to theta's scale.
+__global__ void __launch_bounds__(256) unscale_kernel(const mps_2q_job* __restrict__ jobs,
+                                                      TwoQGeom g) {
+    const int j = blockIdx.y;
+    const int e = g.scale[j];
+    if (e == 0) return;
+    const mps_2q_job job = jobs[j];
+    const float f = ldexpf(1.f, -e);
+    const size_t m = (size_t)job.chi_l * g.d, n = (size_t)g.d * job.chi_r;
+    const size_t r = m < n ? m : n, k = (size_t)job.k;
+    cf* out = reinterpret_cast<cf*>(job.keep_left_canonical ? job.b_out : job.a_out);
+    const size_t count = out ? (job.keep_left_canonical ? k * n : m * k) : 0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count;
+         t += (size_t)gridDim.x * blockDim.x)
+        out[t] = cscale(out[t], f);
+    if (blockIdx.x == 0) {
+        if (job.svals)
+            for (size_t t = threadIdx.x; t < r; t += blockDim.x) job.svals[t] *= f;
+        if (job.discarded && threadIdx.x == 0) *job.discarded = ldexp(*job.discarded, -2 * e);
+    }
+}
+
+int scale_theta(const mps_2q_job* jobs, int njobs, const TwoQGeom& g, cudaStream_t s) {
+    MPS_CUDA_CHECK(cudaMemsetAsync(g.nrm2, 0, (size_t)njobs * sizeof(double), s));
+    const size_t count = (size_t)g.lslot * g.cslot;
+    const int bx = (int)((count + 256 * 32 - 1) / (256 * 32));
+    dim3 grid(bx < 1 ? 1 : bx, njobs);
+    theta_norm_kernel<<<grid, 256, 0, s>>>(g);
+    MPS_LAUNCH_CHECK("theta_norm_kernel");
+    theta_scale_kernel<<<grid, 256, 0, s>>>(jobs, g);
+    MPS_LAUNCH_CHECK("theta_scale_kernel");
+    return MPS_OK;
+}
+
+int unscale_outputs(const mps_2q_job* jobs, int njobs, int max_m, int max_n, const TwoQGeom& g,
+                    cudaStream_t s) {
+    const size_t count = (size_t)max_m * max_n;
+    const int bx = (int)((count + 256 * 16 - 1) / (256 * 16));
+    unscale_kernel<<<dim3(bx < 1 ? 1 : bx, njobs), 256, 0, s>>>(jobs, g);
+    MPS_LAUNCH_CHECK("unscale_kernel");
+    return MPS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Launch helpers.
 
 // Largest dynamic shared memory a kernel may request on the current device:
@@ -1217,7 +1317,7 @@ visit_fn pick_visit(int lw, int* bc) {
 struct Layout {
     int lslot, cslot;
     size_t off_X, off_X2, off_V, off_V2, off_T, off_sig, off_perm, off_off, off_done, off_need,
-        off_counter, off_sync, total;
+        off_counter, off_scale, off_nrm2, off_sync, total;
     int nbmax;
 };
 
@@ -1248,6 +1348,8 @@ Layout make_layout(int njobs, int max_m, int max_n) {
     lo.off_done = o; o = align_up(o + nj * sizeof(int), 256);
     lo.off_need = o; o = align_up(o + nj * sizeof(int), 256);
     lo.off_counter = o; o = align_up(o + 4 * sizeof(int), 256);
+    lo.off_scale = o; o = align_up(o + nj * sizeof(int), 256);
+    lo.off_nrm2 = o; o = align_up(o + nj * sizeof(double), 256);
     // sweep sync: next_item, error, then block_round[njobs][nbmax] (nbmax
     // for the smallest block width, 8 columns)
     lo.nbmax = (int)align_up((size_t)(lo.cslot + 7) / 8, 2);
@@ -1302,6 +1404,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     g.done = reinterpret_cast<int*>(ws + lo.off_done);
     g.need = reinterpret_cast<int*>(ws + lo.off_need);
     g.counter = reinterpret_cast<int*>(ws + lo.off_counter);
+    g.scale = reinterpret_cast<int*>(ws + lo.off_scale);
+    g.nrm2 = reinterpret_cast<double*>(ws + lo.off_nrm2);
 
     int max_sweeps = 40;
     float tol = 0.f;
@@ -1343,6 +1447,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     }
     const int max_chil = (max_m + d - 1) / d, max_chir = (max_n + d - 1) / d;
     int rc = merge_gate_launch(jobs, njobs, max_chil, max_chir, g, s);
+    if (rc) return rc;
+    rc = scale_theta(jobs, njobs, g, s);
     if (rc) return rc;
 
     const int cmax = min(max_m, max_n);
@@ -1423,6 +1529,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         complete_kernel<<<njobs, COMP_T, comp_smem, s>>>(jobs, g);
         MPS_LAUNCH_CHECK("complete_kernel");
         rc = launch_post(jobs, njobs, max_m, max_n, kmax, g, s);
+        if (rc) return rc;
+        rc = unscale_outputs(jobs, njobs, max_m, max_n, g, s);
         if (rc) return rc;
     }
     MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 1, g.counter + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1517,6 +1625,8 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     g.done = reinterpret_cast<int*>(ws + lo.off_done);
     g.need = reinterpret_cast<int*>(ws + lo.off_need);
     g.counter = reinterpret_cast<int*>(ws + lo.off_counter);
+    g.scale = reinterpret_cast<int*>(ws + lo.off_scale);
+    g.nrm2 = reinterpret_cast<double*>(ws + lo.off_nrm2);
 
     int max_sweeps = 40;
     float tol = 0.f;
@@ -1545,6 +1655,8 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     }
     const int max_chil = (max_m + d - 1) / d, max_chir = (max_n + d - 1) / d;
     rc = merge_gate_launch(jobs, njobs, max_chil, max_chir, g, s);
+    if (rc) return rc;
+    rc = scale_theta(jobs, njobs, g, s);
     if (rc) return rc;
 
     const int cmax = min(max_m, max_n);
@@ -1613,6 +1725,8 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
         complete_kernel<<<njobs, COMP_T, comp_smem, s>>>(jobs, g);
         MPS_LAUNCH_CHECK("complete_kernel");
         rc = launch_post(jobs, njobs, max_m, max_n, kmax, g, s);
+        if (rc) return rc;
+        rc = unscale_outputs(jobs, njobs, max_m, max_n, g, s);
         if (rc) return rc;
     }
     MPS_CUDA_CHECK(cudaMemcpyAsync(host_counter + 1, g.counter + 1, sizeof(int),

@@ -133,3 +133,22 @@ def test_64q_chi256_against_oracle(cuda):
     n_ref = float(z["oracle_c128_norm"])
     n64 = float(z["oracle_c64_norm"])
     assert abs(mps.norm() - n_ref) / n_ref < max(10 * abs(n64 - n_ref) / n_ref, 1e-3)
+
+
+def test_tiny_norm_state_matches_unit_norm(cuda):
+    """A state renormalised to 1e-14 (squared column norms near 1e-30, inner
+    products below FP32's normal range) must evolve like the unit-norm one:
+    the kernel scales every theta by a power of two before its SVD."""
+    circ = C.brickwork(10, 8, d=2, maxsvals=16, seed=5)
+    a, b = MPS(10), MPS(10)
+    ratio = None
+    for t, lay in enumerate(circ.layers):
+        a.apply_layer(lay.one_q, lay.pair_left, lay.two_q, maxsvals=16)
+        b.apply_layer(lay.one_q, lay.pair_left, lay.two_q, maxsvals=16)
+        if t == 2:
+            ratio = 1e-14 / a.norm()
+            b.renormalize(1e-14)
+    assert list(a.bond_dimensions()) == list(b.bond_dimensions())
+    wa, wb = a.wavefunction(), b.wavefunction()
+    assert infidelity(wa, wb) < 1e-9
+    assert abs(b.norm() / a.norm() / ratio - 1.0) < 1e-4

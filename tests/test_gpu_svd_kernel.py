@@ -158,6 +158,19 @@ def test_full_size_job(built_lib, cuda, chi, d, k):
         assert p.sweeps_out < 40
 
 
+@pytest.mark.parametrize("scale", [1e-20, 1e-9, 1e15])
+def test_scale_invariance(built_lib, cuda, scale):
+    """theta scaled far from 1: squared norms of 1e-40 are below FP32's
+    normal range unless the kernel rescales theta (exactly, by a power of
+    two) before the SVD; the same relative tolerances must hold."""
+    rng = np.random.default_rng(17)
+    for lc in (True, False):
+        a, b, g = make_job_inputs(rng, 64, 64, 64, 2, scale=scale / 64)
+        rc, res, _ = run_batch(built_lib, cuda, [(a, b, g, 100, lc)])
+        assert rc == 0, _native.last_error()
+        check_job((a, b, g, 100, lc), res[0], 2)
+
+
 def test_batch_equals_single(built_lib, cuda):
     rng = np.random.default_rng(7)
     specs = []
