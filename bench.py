@@ -121,24 +121,11 @@ class Clocks:
 
 
 def circuit_shapes(circ):
-    """Counts of (chi_l, chi_m, chi_r) over the circuit's two-qudit gates and of
-    (chi_l, chi_r) over its one-qudit gates.  Bond dimensions are fixed by the
-    circuit (kept count = min(maxsvals, min(chi_l d, d chi_r))), so no
-    simulation is needed."""
-    from collections import Counter
-    from mpsim_gb300.core import kept_count
-    n, d = circ.nqudits, circ.d
-    bonds = [1] * (n + 1)
-    two, one = Counter(), Counter()
-    for lay in circ.layers:
-        for i in range(n):
-            one[(bonds[i], bonds[i + 1])] += 1
-        for i in lay.pair_left:
-            i = int(i)
-            cl, cm, cr = bonds[i], bonds[i + 1], bonds[i + 2]
-            two[(cl, cm, cr)] += 1
-            bonds[i + 1] = kept_count(circ.maxsvals, min(cl * d, d * cr))
-    return one, two
+    """Counts of (chi_l, chi_r) over the circuit's one-qudit gates and of
+    (chi_l, chi_m, chi_r) over its two-qudit gates (the deterministic shape
+    plan of mpsim_gb300.circuits.gate_shapes)."""
+    from mpsim_gb300.circuits import gate_shapes
+    return gate_shapes(circ)
 
 
 def _time_call(fn, min_seconds=0.02):
@@ -250,7 +237,10 @@ def circ_name(circ):
 
 def run_batch_workload(args, rank, world):
     """Multi-circuit workloads: batch_512_mixed and qutrit_128x32_d30_chi192.
-    A step is every circuit of the batch from |0...0> to its last layer."""
+    A step is every circuit of the batch from |0...0> to its last layer.  With
+    several ranks the one batch is sharded by estimated cost
+    (circuits.shard_by_cost: circuits are independent, no collective on the
+    data path) and the step time is the slowest rank's: strong scaling."""
     import torch
     import __graft_entry__ as ge
     from mpsim_gb300 import circuits as C
@@ -258,44 +248,71 @@ def run_batch_workload(args, rank, world):
     from mpsim_gb300.batch import run_circuits
 
     ge.build()
-    torch.cuda.set_device(0)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
     if args.workload == "batch_512_mixed":
-        circs = C.mixed_batch(args.ncircuits or 512, seed=replica_instance(rank))
+        every = C.mixed_batch(args.ncircuits or 512, seed=0)
     else:
-        circs = C.qutrit_batch(args.ncircuits or 128, seed=replica_instance(rank))
-    ngates = sum(c.n_two_qudit_gates for c in circs)
+        every = C.qutrit_batch(args.ncircuits or 128, seed=0)
+    mine = C.shard_by_cost(every, world)[rank]
+    circs = [every[i] for i in mine]
+    ngates_all = sum(c.n_two_qudit_gates for c in every)
     lib = _native.load()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
     for _ in range(args.warmup):
         flush.fill_(1)
-        run_circuits(circs)
-    torch.cuda.synchronize()
-    clocks = Clocks(0)
+        if circs:
+            run_circuits(circs)
+    barrier()
+    clocks = Clocks(local)
     clocks.start()
     l0 = lib.mps_kernel_launches()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record()
+    states = []
     for _ in range(args.steps):
         flush.fill_(1)
-        states = run_circuits(circs)
+        if circs:
+            states = run_circuits(circs)
     e1.record()
-    torch.cuda.synchronize()
+    barrier()
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
-    line = {
-        "metric": f"two-qudit gates/s ({args.workload})", "value": ngates * args.steps / (ms / 1000.0),
-        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded Haar gates)",
-        "config": {"workload": args.workload, "circuits": len(circs),
-                   "two_qudit_gates_per_step": ngates,
-                   "l2": "256 MiB buffer written at the start of every step"},
-        "circuits_per_s": len(circs) * args.steps / (ms / 1000.0),
-        "gpu_launches": int(lib.mps_kernel_launches() - l0), "clocks": clk,
-        "mean_norm": float(np.mean([s.norm() for s in states])),
-    }
-    print(json.dumps(line), flush=True)
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    if rank == 0:
+        line = {
+            "metric": f"two-qudit gates/s ({args.workload})",
+            "value": ngates_all * args.steps / (ms / 1000.0),
+            "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded Haar gates)",
+            "config": {"workload": args.workload, "circuits": len(every),
+                       "two_qudit_gates_per_step": ngates_all,
+                       "parallelism": f"cost-sharded x{world}",
+                       "l2": "256 MiB buffer written at the start of every step"},
+            "circuits_per_s": len(every) * args.steps / (ms / 1000.0),
+            "gpu_launches": int(lib.mps_kernel_launches() - l0), "clocks": clk,
+            "mean_norm": float(np.mean([s.norm() for s in states])) if states else None,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
     return 0
 
 

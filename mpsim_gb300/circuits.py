@@ -18,7 +18,7 @@ Workloads (qubit count, depth, truncation) named by their sizes:
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import List, Optional
+from typing import List, Optional, Sequence
 
 import numpy as np
 
@@ -120,6 +120,57 @@ def mixed_batch(ncircuits: int = 512, seed: int = 0) -> List[BrickworkCircuit]:
 def qutrit_batch(ncircuits: int = 128, seed: int = 0) -> List[BrickworkCircuit]:
     """128 circuits of 32 qutrits, depth 30, maxsvals=192 (theta <= 576x576)."""
     return [brickwork(32, 30, 3, 192, seed, k) for k in range(ncircuits)]
+
+
+def gate_shapes(circ: BrickworkCircuit):
+    """(one-qudit, two-qudit) Counters of (chi_l, chi_r) and (chi_l, chi_m,
+    chi_r) over the circuit's gates.  The kept count of every two-qudit gate
+    is min(maxsvals, min(chi_l d, d chi_r)), so the whole shape plan follows
+    from the circuit without simulating it."""
+    from collections import Counter
+    n, d = circ.nqudits, circ.d
+    bonds = [1] * (n + 1)
+    two, one = Counter(), Counter()
+    for lay in circ.layers:
+        for i in range(n):
+            one[(bonds[i], bonds[i + 1])] += 1
+        for i in lay.pair_left:
+            i = int(i)
+            cl, cm, cr = bonds[i], bonds[i + 1], bonds[i + 2]
+            two[(cl, cm, cr)] += 1
+            r = min(cl * d, d * cr)
+            bonds[i + 1] = r if circ.maxsvals is None else min(int(circ.maxsvals), r)
+    return one, two
+
+
+def estimated_cost(circ: BrickworkCircuit) -> float:
+    """Relative device cost of a circuit: per two-qudit gate, the Jacobi SVD's
+    L C^2 (L = max(m, n) rows, C = min(m, n) columns of the merged matrix) plus
+    the merge's m n chi_m."""
+    d = circ.d
+    _, two = gate_shapes(circ)
+    total = 0.0
+    for (cl, cm, cr), count in two.items():
+        m, n = cl * d, d * cr
+        total += count * (max(m, n) * min(m, n) ** 2 + m * n * cm)
+    return total
+
+
+def shard_by_cost(circuits: Sequence[BrickworkCircuit], world: int) -> List[List[int]]:
+    """Indices of ``circuits`` for each of ``world`` ranks: longest estimated
+    cost first, each to the rank with the least work so far (every circuit
+    exactly once; ranks may be empty when there are fewer circuits)."""
+    if world < 1:
+        raise ValueError("world must be at least 1")
+    costs = [estimated_cost(c) for c in circuits]
+    order = sorted(range(len(circuits)), key=lambda i: (-costs[i], i))
+    loads = [0.0] * world
+    shards = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda q: (loads[q], q))
+        shards[r].append(i)
+        loads[r] += costs[i]
+    return [sorted(s) for s in shards]
 
 
 def sample_bitstrings(nqudits: int, d: int, count: int = 4096, seed: int = 0) -> np.ndarray:

@@ -172,3 +172,17 @@ def test_job_struct_layout_matches_header(tmp_path):
     assert off_chil == dt.fields["chi_l"][1]
     assert off_k == dt.fields["k"][1]
     assert psize == ctypes.sizeof(_native.SvdParams)
+
+
+def test_shape_plan_and_cost_shards():
+    from mpsim_gb300 import circuits as C
+    circ = C.workload("brickwork_64q_d40_chi256")
+    one, two = C.gate_shapes(circ)
+    assert sum(two.values()) == circ.n_two_qudit_gates == 1260
+    assert sum(one.values()) == 64 * 40
+    assert max(two) == (256, 256, 256)
+    batch = C.qutrit_batch(8)
+    shards = C.shard_by_cost(batch, 3)
+    assert sorted(i for s in shards for i in s) == list(range(8))
+    assert C.shard_by_cost(batch, 1) == [list(range(8))]
+    assert [len(s) for s in C.shard_by_cost(batch[:2], 4)].count(0) == 2

@@ -58,3 +58,39 @@ def test_two_replicas_over_gloo():
     assert n0 == n1 == 8
     assert rate0 == rate1 == 2 * n0 / (mx0 / 1000.0)
     assert g0 != g1            # each rank simulates its own circuit instance
+
+
+def _shard_worker(rank, world, port, out):
+    import torch
+    import torch.distributed as dist
+    from mpsim_gb300 import circuits as C
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    every = C.mixed_batch(64, seed=0)
+    mine = C.shard_by_cost(every, world)[rank]
+    cost = sum(C.estimated_cost(every[i]) for i in mine)
+    t = torch.tensor([cost], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    out.put((rank, mine, cost, float(t.item())))
+    dist.destroy_process_group()
+
+
+def test_batch_sharded_by_cost_over_gloo():
+    """The multi-circuit bench path with two ranks: every circuit on exactly
+    one rank, the ranks' estimated work within 10% of each other, and the
+    slowest rank's figure reduced with MAX."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_shard_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in range(2))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (_, m0, c0, x0), (_, m1, c1, x1) = res
+    assert sorted(m0 + m1) == list(range(64))
+    assert not set(m0) & set(m1)
+    assert x0 == x1 == max(c0, c1)
+    assert max(c0, c1) / min(c0, c1) < 1.10
