@@ -47,6 +47,12 @@ def gate_flops(m, n, chim, d):
     return 8.0 * m * n * chim + 8.0 * m * n * d * d + 4.0 * (14.0 * big * small ** 2 + 8.0 * small ** 3)
 
 
+# DRAM bytes (read + write) of one mps_apply_2q_batch call on a chi=256 layer of
+# the default workload, summed over its 69 launches from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/traffic_2q_call_chi256.md).
+CALL_TRAFFIC_BYTES = 3.0625e9
+
+
 def replica_instance(rank: int) -> int:
     """Circuit instance simulated by a rank (replicas: one per GPU)."""
     return rank
@@ -463,7 +469,8 @@ def main():
                        "l2": "256 MiB buffer written at the start of every step"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
-                         "traffic": None,
+                         "traffic": CALL_TRAFFIC_BYTES if args.workload == WORKLOAD else None,
+                         "traffic_unit": "bytes per call (one chi=256 layer, 32 gates)",
                          "kernel": "mps_apply_2q_batch on chi=256 layers (merge + Jacobi SVD + "
                                    "regauge, all launches of one call)",
                          "flops_per_gate": f_gate, "peak_source": f"bf16 sustained ({peak_kind})",
