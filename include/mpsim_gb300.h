@@ -113,7 +113,9 @@ size_t mps_2q_workspace_bytes(int njobs, int max_m, int max_n, int d);
  * Jacobi SVD, descending sort, truncation to k values, and the regauge with
  * the singular values placed as keep_left_canonical asks.  max_m/max_n bound
  * every job's theta; the host must know them.  Blocks the calling thread
- * once per Jacobi sweep to test convergence.
+ * once per Jacobi sweep to test convergence, and returns after the last
+ * sweep with the sort, regauge and output kernels still queued on the stream
+ * (the outputs are stream-ordered like any kernel's).
  * Replaces MPS.apply_two_qudit_gate for adjacent sites (mpsim/core.py:
  * 1059-1152: merge 1059-1062, gate 1064-1068, truncated SVD 1132-1137 via
  * TensorNetwork split_node_full_svd, S placement 1139-1145). */

@@ -1133,8 +1133,14 @@ __device__ __forceinline__ int theta_scale_exponent(double n2) {
 __global__ void __launch_bounds__(256) theta_scale_kernel(const mps_2q_job* __restrict__ jobs,
                                                           TwoQGeom g) {
     const int j = blockIdx.y;
-    const int e = theta_scale_exponent(g.nrm2[j]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) g.scale[j] = e;
+    const double n2 = g.nrm2[j];
+    const int e = theta_scale_exponent(n2);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        g.scale[j] = e;
+        // a NaN/Inf element makes |theta|^2 non-finite; the scaled Jacobi
+        // arithmetic cannot create one, so this is the call's whole check
+        if (!isfinite(n2)) atomicAdd(g.counter + 1, 1);
+    }
     if (e == 0) return;
     const float f = ldexpf(1.f, e);
     const size_t count = (size_t)g.lslot * g.cslot;
@@ -1485,7 +1491,7 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
             if (rc) return rc;
             sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
-            MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, sizeof(int),
+            MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, 2 * sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
             MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 2, sync.error, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
@@ -1533,8 +1539,16 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         rc = unscale_outputs(jobs, njobs, max_m, max_n, g, s);
         if (rc) return rc;
     }
-    MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 1, g.counter + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MPS_CUDA_CHECK(cudaStreamSynchronize(s));
+    // The non-finite count is complete before the first sweep (see
+    // theta_scale_kernel) and came back with every convergence read, so the
+    // call returns without waiting for its last kernels and the host can
+    // prepare the next call meanwhile.  Jobs of one column have no sweep: read
+    // the count here.
+    if (cmax < 2) {
+        MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 1, g.counter + 1, sizeof(int),
+                                       cudaMemcpyDeviceToHost, s));
+        MPS_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
     if (t_pinned[1] != 0) return fail(MPS_ERR_NONFINITE, "mps_apply_2q_batch: NaN/Inf singular value");
     if (!converged)
         return fail(MPS_ERR_NOT_CONVERGED, "mps_apply_2q_batch: Jacobi SVD hit its sweep cap");
