@@ -133,7 +133,7 @@ int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs_dev, int njobs,
  * Same jobs, same results; scratch comes from a static __device__ array of
  * MPS_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
  * exit, and the call allocates nothing.  Jobs whose slots need more scratch
- * than that are rejected with MPS_ERR_WORKSPACE (at theta 512x512 about three
+ * than that are rejected with MPS_ERR_WORKSPACE (at theta 512x512 about five
  * jobs fit per call).  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress) with that device current: make it before any
  * stream capture.  Calls share the array: calls that overlap on the GPU race

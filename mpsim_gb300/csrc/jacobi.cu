@@ -145,20 +145,31 @@ __device__ __forceinline__ int block_col(int c, int I, int J, int BC) {
     return (c < BC) ? I * BC + c : J * BC + (c - BC);
 }
 
+// Physical column of job j at sorted position c.  The columns are never
+// moved: the per-sweep norm sort rewrites this map instead (positions >= C,
+// the zero padding, always map to themselves).
+__device__ __forceinline__ int phys_col(const TwoQGeom& g, int j, int c) {
+    return __ldcg(g.cmap + (size_t)j * g.cslot + c);
+}
+
 // V <- V Q for the 2*BC columns of this visit (rows < C).
 template <int BC>
-__device__ __forceinline__ void update_v(cf* V, int cslot, int C, int I, int J, const cf* Qs) {
+__device__ __forceinline__ void update_v(const TwoQGeom& g, int j, int C, int I, int J,
+                                         const cf* Qs) {
     constexpr int W = 2 * BC;
+    const int cslot = g.cslot;
+    cf* V = g.V + (size_t)j * cslot * cslot;
     for (int r = threadIdx.x; r < C; r += BC * 32) {
         cf v[W];
 #pragma unroll
-        for (int c = 0; c < W; ++c) v[c] = __ldcg(V + (size_t)block_col(c, I, J, BC) * cslot + r);
+        for (int c = 0; c < W; ++c)
+            v[c] = __ldcg(V + (size_t)phys_col(g, j, block_col(c, I, J, BC)) * cslot + r);
 #pragma unroll 4
         for (int c2 = 0; c2 < W; ++c2) {
             cf acc = cmake(0.f, 0.f);
 #pragma unroll
             for (int c = 0; c < W; ++c) cfma(acc, v[c], Qs[c2 * W + c]);
-            V[(size_t)block_col(c2, I, J, BC) * cslot + r] = acc;
+            V[(size_t)phys_col(g, j, block_col(c2, I, J, BC)) * cslot + r] = acc;
         }
     }
 }
@@ -200,7 +211,7 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int c = warp; c < W; c += BC) {
-        const cf* src = X + (size_t)block_col(c, I, J, BC) * g.lslot;
+        const cf* src = X + (size_t)phys_col(g, j, block_col(c, I, J, BC)) * g.lslot;
         for (int r = lane; r < Lw; r += 32) Xs[(size_t)c * Lw + r] = __ldcg(src + r);
     }
     if (sh.track_v)
@@ -267,10 +278,12 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
         __syncthreads();
     }
     for (int c = warp; c < W; c += BC) {
-        cf* dst = X + (size_t)block_col(c, I, J, BC) * g.lslot;
+        const int pc = phys_col(g, j, block_col(c, I, J, BC));
+        cf* dst = X + (size_t)pc * g.lslot;
         for (int r = lane; r < Lw; r += 32) dst[r] = Xs[(size_t)c * Lw + r];
+        if (lane == 0) g.cnrm[(size_t)j * g.cslot + pc] = nrm[c];
     }
-    if (sh.track_v) update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
+    if (sh.track_v) update_v<BC>(g, j, sh.C, I, J, Qs);
     publish_offmax(offmax, s_off, BC, g.offmax + j);
 }
 
@@ -309,8 +322,8 @@ __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, 
     cf hx[ROWS], vx[ROWS];
     float hn = 0.f, vn = 0.f;
     {
-        const cf* hs = X + (size_t)(I * BC + warp) * g.lslot;
-        const cf* vs = X + (size_t)(J * BC + warp) * g.lslot;
+        const cf* hs = X + (size_t)phys_col(g, j, I * BC + warp) * g.lslot;
+        const cf* vs = X + (size_t)phys_col(g, j, J * BC + warp) * g.lslot;
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
             hx[i] = __ldcg(hs + lane + 32 * i);
@@ -386,17 +399,22 @@ __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, 
         }
     }
     {
-        cf* hd = X + (size_t)(I * BC + warp) * g.lslot;
-        cf* vd = X + (size_t)(J * BC + vid) * g.lslot;
+        const int ph = phys_col(g, j, I * BC + warp), pv = phys_col(g, j, J * BC + vid);
+        cf* hd = X + (size_t)ph * g.lslot;
+        cf* vd = X + (size_t)pv * g.lslot;
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
             hd[lane + 32 * i] = hx[i];
             vd[lane + 32 * i] = vx[i];
         }
+        if (lane == 0) {
+            g.cnrm[(size_t)j * g.cslot + ph] = hn;
+            g.cnrm[(size_t)j * g.cslot + pv] = vn;
+        }
     }
     if (sh.track_v) {
         __syncthreads();
-        update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
+        update_v<BC>(g, j, sh.C, I, J, Qs);
     }
     publish_offmax(offmax, s_off, BC, g.offmax + j);
 }
@@ -446,8 +464,8 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
     cf hx[ROWS], vx[ROWS];
     float hn = 0.f;
     {
-        const cf* hs = X + (size_t)(I * BC + warp) * g.lslot;
-        const cf* vs = X + (size_t)(J * BC + warp) * g.lslot;
+        const cf* hs = X + (size_t)phys_col(g, j, I * BC + warp) * g.lslot;
+        const cf* vs = X + (size_t)phys_col(g, j, J * BC + warp) * g.lslot;
         cf* vd = vis + (size_t)warp * LW;
         float vn = 0.f;
 #pragma unroll
@@ -530,9 +548,10 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
     parity ^= 1u;
     if (expired && lane == 0) atomicExch(err, 1);
     const bool any = __syncthreads_or(rotated ? 1 : 0) != 0;
+    const int ph = phys_col(g, j, I * BC + warp), pv = phys_col(g, j, J * BC + warp);
     if (any) {
-        cf* hd = X + (size_t)(I * BC + warp) * g.lslot;
-        cf* vd = X + (size_t)(J * BC + warp) * g.lslot;
+        cf* hd = X + (size_t)ph * g.lslot;
+        cf* vd = X + (size_t)pv * g.lslot;
         const cf* vsrc = vis + (size_t)warp * LW;
 #pragma unroll
         for (int i = 0; i < ROWS; ++i) {
@@ -540,7 +559,11 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
             vd[lane + 32 * i] = vsrc[lane + 32 * i];
         }
     }
-    if (sh.track_v && any) update_v<BC>(g.V + (size_t)j * g.cslot * g.cslot, g.cslot, sh.C, I, J, Qs);
+    if (lane == 0) {       // the norms the next sweep's sort reads
+        g.cnrm[(size_t)j * g.cslot + ph] = hn;
+        g.cnrm[(size_t)j * g.cslot + pv] = visn[warp];
+    }
+    if (sh.track_v && any) update_v<BC>(g, j, sh.C, I, J, Qs);
     publish_offmax(offmax, s_off, BC, g.offmax + j);
 }
 
@@ -640,9 +663,9 @@ __global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol2) {
     g.offmax[j] = 0.f;
 }
 
-__global__ void init_slots_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, cf* V2,
-                                  int njobs) {
-    // both V buffers = identity for jobs that track V; bookkeeping cleared
+__global__ void init_slots_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int njobs) {
+    // V = identity for jobs that track V, identity column maps, bookkeeping
+    // cleared
     const size_t per = (size_t)g.cslot * g.cslot;
     const size_t total = per * njobs;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
@@ -654,8 +677,10 @@ __global__ void init_slots_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom 
         const int r = (int)(w % g.cslot), c = (int)(w / g.cslot);
         const cf v = (r == c) ? cmake(1.f, 0.f) : cmake(0.f, 0.f);
         g.V[e] = v;
-        V2[e] = v;
     }
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)njobs * g.cslot;
+         e += (size_t)gridDim.x * blockDim.x)
+        g.cmap[e] = (int)(e % g.cslot);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < njobs) {
         g.done[t] = 0;
@@ -667,8 +692,10 @@ __global__ void init_slots_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom 
 
 // ---------------------------------------------------------------------------
 // Per-sweep reordering: columns sorted by descending norm before each sweep
-// (de Rijk's ordering), which cuts the sweep count.  presort_kernel writes the
-// permutation; gather_kernel copies X (and V) columns into the other buffer.
+// (de Rijk's ordering), which cuts the sweep count.  The columns stay where
+// they are; presort_kernel sorts the squared norms the previous sweep's visits
+// left in cnrm (theta_norm_kernel's before the first sweep) and rewrites the
+// job's column map.  Converged jobs keep theirs.
 constexpr int PRESORT_T = 512;
 
 __global__ void __launch_bounds__(PRESORT_T)
@@ -676,23 +703,21 @@ presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2) {
     extern __shared__ float2 sm1[];
     float* key = reinterpret_cast<float*>(sm1);
     int* idx = reinterpret_cast<int*>(key + npow2);
-    // Every job is reordered, converged or not, so the two buffers never
-    // disagree about where a job's columns live.
     const int j = blockIdx.x;
+    if (__ldg(g.done + j)) return;
     const int m = jobs[j].chi_l * g.d, n = jobs[j].chi_r * g.d;
-    const int L = max(m, n), C = min(m, n);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const cf* X = g.X + (size_t)j * g.lslot * g.cslot;
+    const int C = min(m, n);
+    if (C < 2) return;
+    const int tid = threadIdx.x;
+    const float* cn = g.cnrm + (size_t)j * g.cslot;
     for (int i = tid; i < npow2; i += PRESORT_T) {
-        key[i] = -1.f;
+        float k = -1.f;
+        if (i < C) {
+            k = cn[i];
+            if (!(k == k)) k = 0.f;                  // NaN sorts as zero
+        }
+        key[i] = k;
         idx[i] = i;
-    }
-    __syncthreads();
-    for (int c = warp; c < C; c += PRESORT_T / 32) {
-        float s = 0.f;
-        for (int r = lane; r < L; r += 32) s += cabs2(X[(size_t)c * g.lslot + r]);
-        s = warp_sum(s);
-        if (lane == 0) key[c] = (s == s) ? s : 0.f;   // NaN sorts as zero
     }
     __syncthreads();
     for (int size = 2; size <= npow2; size <<= 1) {
@@ -713,27 +738,7 @@ presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2) {
             __syncthreads();
         }
     }
-    for (int i = tid; i < C; i += PRESORT_T) g.perm[(size_t)j * g.cslot + i] = idx[i];
-}
-
-// dst column c = src column perm[c] for c < C (X: Lw rows; V: C rows).
-__global__ void gather_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, cf* Xdst,
-                              cf* Vdst) {
-    const int j = blockIdx.y;
-    const int m = jobs[j].chi_l * g.d, n = jobs[j].chi_r * g.d;
-    const int L = max(m, n), C = min(m, n);
-    const int c = blockIdx.x;
-    if (c >= C) return;
-    const int src = g.perm[(size_t)j * g.cslot + c];
-    const int Lw = (L + 31) & ~31;
-    const cf* xs = g.X + (size_t)j * g.lslot * g.cslot + (size_t)src * g.lslot;
-    cf* xd = Xdst + (size_t)j * g.lslot * g.cslot + (size_t)c * g.lslot;
-    for (int r = threadIdx.x; r < Lw; r += blockDim.x) xd[r] = xs[r];
-    if (job_tracks_v(m, n, jobs[j].keep_left_canonical)) {
-        const cf* vs = g.V + (size_t)j * g.cslot * g.cslot + (size_t)src * g.cslot;
-        cf* vd = Vdst + (size_t)j * g.cslot * g.cslot + (size_t)c * g.cslot;
-        for (int r = threadIdx.x; r < C; r += blockDim.x) vd[r] = vs[r];
-    }
+    for (int i = tid; i < C; i += PRESORT_T) g.cmap[(size_t)j * g.cslot + i] = idx[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -1102,24 +1107,25 @@ complete_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
 // which the reference uses, scales for the same reason.  Multiplying by a
 // power of two changes no bit of the relative arithmetic.
 
+// Warp per column: squared column norms (FP64 sums) into cnrm, for the first
+// sweep's norm sort, and |theta|_F^2 into nrm2.
 __global__ void __launch_bounds__(256) theta_norm_kernel(TwoQGeom g) {
-    __shared__ double part[256];
     const int j = blockIdx.y;
-    const size_t count = (size_t)g.lslot * g.cslot;
-    const cf* X = g.X + (size_t)j * count;
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (c >= g.cslot) return;
+    const cf* col = g.X + (size_t)j * g.lslot * g.cslot + (size_t)c * g.lslot;
     double acc = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const cf x = X[t];
+    for (int r = lane; r < g.lslot; r += 32) {
+        const cf x = col[r];
         acc += (double)x.x * x.x + (double)x.y * x.y;
     }
-    part[threadIdx.x] = acc;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
-        __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+        g.cnrm[(size_t)j * g.cslot + c] = (float)acc;
+        if (acc != 0.0) atomicAdd(g.nrm2 + j, acc);
     }
-    if (threadIdx.x == 0) atomicAdd(g.nrm2 + j, part[0]);
 }
 
 __device__ __forceinline__ int theta_scale_exponent(double n2) {
@@ -1180,11 +1186,11 @@ __global__ void __launch_bounds__(256) unscale_kernel(const mps_2q_job* __restri
 
 int scale_theta(const mps_2q_job* jobs, int njobs, const TwoQGeom& g, cudaStream_t s) {
     MPS_CUDA_CHECK(cudaMemsetAsync(g.nrm2, 0, (size_t)njobs * sizeof(double), s));
+    theta_norm_kernel<<<dim3((g.cslot + 7) / 8, njobs), 256, 0, s>>>(g);
+    MPS_LAUNCH_CHECK("theta_norm_kernel");
     const size_t count = (size_t)g.lslot * g.cslot;
     const int bx = (int)((count + 256 * 32 - 1) / (256 * 32));
     dim3 grid(bx < 1 ? 1 : bx, njobs);
-    theta_norm_kernel<<<grid, 256, 0, s>>>(g);
-    MPS_LAUNCH_CHECK("theta_norm_kernel");
     theta_scale_kernel<<<grid, 256, 0, s>>>(jobs, g);
     MPS_LAUNCH_CHECK("theta_scale_kernel");
     return MPS_OK;
@@ -1322,7 +1328,7 @@ visit_fn pick_visit(int lw, int* bc) {
 
 struct Layout {
     int lslot, cslot;
-    size_t off_X, off_X2, off_V, off_V2, off_T, off_sig, off_perm, off_off, off_done, off_need,
+    size_t off_X, off_V, off_T, off_sig, off_perm, off_cmap, off_cnrm, off_off, off_done, off_need,
         off_counter, off_scale, off_nrm2, off_sync, total;
     int nbmax;
 };
@@ -1344,12 +1350,12 @@ Layout make_layout(int njobs, int max_m, int max_n) {
     size_t o = 0;
     const size_t nj = (size_t)max(njobs, 1);
     lo.off_X = o; o = align_up(o + nj * lo.lslot * lo.cslot * sizeof(cf), 256);
-    lo.off_X2 = o; o = align_up(o + nj * lo.lslot * lo.cslot * sizeof(cf), 256);
     lo.off_V = o; o = align_up(o + nj * lo.cslot * lo.cslot * sizeof(cf), 256);
-    lo.off_V2 = o; o = align_up(o + nj * lo.cslot * lo.cslot * sizeof(cf), 256);
     lo.off_T = o; o = align_up(o + nj * lo.lslot * lo.cslot * sizeof(cf), 256);
     lo.off_sig = o; o = align_up(o + nj * lo.cslot * sizeof(float), 256);
     lo.off_perm = o; o = align_up(o + nj * lo.cslot * sizeof(int), 256);
+    lo.off_cmap = o; o = align_up(o + nj * lo.cslot * sizeof(int), 256);
+    lo.off_cnrm = o; o = align_up(o + nj * lo.cslot * sizeof(float), 256);
     lo.off_off = o; o = align_up(o + nj * sizeof(float), 256);
     lo.off_done = o; o = align_up(o + nj * sizeof(int), 256);
     lo.off_need = o; o = align_up(o + nj * sizeof(int), 256);
@@ -1410,6 +1416,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     g.done = reinterpret_cast<int*>(ws + lo.off_done);
     g.need = reinterpret_cast<int*>(ws + lo.off_need);
     g.counter = reinterpret_cast<int*>(ws + lo.off_counter);
+    g.cmap = reinterpret_cast<int*>(ws + lo.off_cmap);
+    g.cnrm = reinterpret_cast<float*>(ws + lo.off_cnrm);
     g.scale = reinterpret_cast<int*>(ws + lo.off_scale);
     g.nrm2 = reinterpret_cast<double*>(ws + lo.off_nrm2);
 
@@ -1440,15 +1448,13 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     sync.wait_limit = (params && params->wait_limit > 0) ? params->wait_limit : (1 << 22);
     sync.stall_test = params ? params->stall_test : 0;
 
-    cf* X2 = reinterpret_cast<cf*>(ws + lo.off_X2);
-    cf* V2 = reinterpret_cast<cf*>(ws + lo.off_V2);
-    // X and X2 back to back: one memset zeroes both (padding rows/columns)
+    // padding rows and columns of X must be zero
     MPS_CUDA_CHECK(cudaMemsetAsync(g.X, 0, lo.off_V - lo.off_X, s));
     {
         const size_t total = (size_t)njobs * lo.cslot * lo.cslot;
         int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
         blocks = max(blocks, (njobs + 255) / 256);
-        init_slots_kernel<<<blocks, 256, 0, s>>>(jobs, g, V2, njobs);
+        init_slots_kernel<<<blocks, 256, 0, s>>>(jobs, g, njobs);
         MPS_LAUNCH_CHECK("init_slots_kernel");
     }
     const int max_chil = (max_m + d - 1) / d, max_chir = (max_n + d - 1) / d;
@@ -1478,10 +1484,6 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
             if (cmax > 2 * bc) {
                 presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2);
                 MPS_LAUNCH_CHECK("presort_kernel");
-                gather_kernel<<<dim3(cmax, njobs), 128, 0, s>>>(jobs, g, X2, V2);
-                MPS_LAUNCH_CHECK("gather_kernel");
-                cf* t = g.X; g.X = X2; X2 = t;
-                t = g.V; g.V = V2; V2 = t;
             }
             // one persistent launch runs every round of the sweep
             MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, 2 * sizeof(int), s));
@@ -1639,6 +1641,8 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     g.done = reinterpret_cast<int*>(ws + lo.off_done);
     g.need = reinterpret_cast<int*>(ws + lo.off_need);
     g.counter = reinterpret_cast<int*>(ws + lo.off_counter);
+    g.cmap = reinterpret_cast<int*>(ws + lo.off_cmap);
+    g.cnrm = reinterpret_cast<float*>(ws + lo.off_cnrm);
     g.scale = reinterpret_cast<int*>(ws + lo.off_scale);
     g.nrm2 = reinterpret_cast<double*>(ws + lo.off_nrm2);
 
@@ -1655,16 +1659,15 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     visit_fn visit = pick_visit(lw, &bc);
     if (params) params->block_cols = bc;
 
-    cf* X2 = reinterpret_cast<cf*>(ws + lo.off_X2);
-    cf* V2 = reinterpret_cast<cf*>(ws + lo.off_V2);
-    // the array keeps the last call's contents: clear X, X2 (padding must be
-    // zero), set V/V2 to I and reset the per-job flags and counters
+    // the array keeps the last call's contents: clear X (padding must be
+    // zero), set V to I, the column maps to identity and reset the per-job
+    // flags and counters
     MPS_CUDA_CHECK(cudaMemsetAsync(g.X, 0, lo.off_V - lo.off_X, s));
     {
         const size_t total = (size_t)njobs * lo.cslot * lo.cslot;
         int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
         blocks = max(blocks, (njobs + 255) / 256);
-        init_slots_kernel<<<blocks, 256, 0, s>>>(jobs, g, V2, njobs);
+        init_slots_kernel<<<blocks, 256, 0, s>>>(jobs, g, njobs);
         MPS_LAUNCH_CHECK("init_slots_kernel");
     }
     const int max_chil = (max_m + d - 1) / d, max_chir = (max_n + d - 1) / d;
@@ -1690,10 +1693,6 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
             if (cmax > 2 * bc) {
                 presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2);
                 MPS_LAUNCH_CHECK("presort_kernel");
-                gather_kernel<<<dim3(cmax, njobs), 128, 0, s>>>(jobs, g, X2, V2);
-                MPS_LAUNCH_CHECK("gather_kernel");
-                cf* t = g.X; g.X = X2; X2 = t;
-                t = g.V; g.V = V2; V2 = t;
             }
             for (int r = 0; r < rounds; ++r) {
                 rc = visit(jobs, njobs, pairs, g, r, tol2, lw, s);

@@ -28,6 +28,8 @@ struct TwoQGeom {
     int* done;        // njobs: 1 once a sweep made no rotation
     int* need;        // njobs: kept columns that need an orthonormal completion
     int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf
+    int* cmap;        // njobs * cslot: physical column at each sorted position
+    float* cnrm;      // njobs * cslot: squared norm of each physical column
     int* scale;       // njobs: theta was multiplied by 2^scale[j] before the SVD
     double* nrm2;     // njobs: |theta|_F^2 (scratch of the scaling)
 };

@@ -116,14 +116,14 @@ def test_noalloc_matches_workspace_entry_point_twice(built_lib, cuda):
 def test_noalloc_rejects_oversized_jobs(built_lib, cuda):
     rng = np.random.default_rng(3)
     big = []
-    for _ in range(4):                      # four theta 512x512 jobs need > 32 MiB
+    for _ in range(8):                      # eight theta 512x512 jobs need > 32 MiB
         a = (rng.normal(size=(256, 2, 256)) + 0j).astype(np.complex64)
         b = (rng.normal(size=(256, 2, 256)) + 0j).astype(np.complex64)
         big.append((a, b, np.eye(4, dtype=np.complex64), 256, True))
     jobs, keep, outs, mm, mn, d = _jobs(cuda, big)
-    assert built_lib.mps_2q_workspace_bytes(4, mm, mn, d) > _native.NOALLOC_SCRATCH_BYTES
+    assert built_lib.mps_2q_workspace_bytes(8, mm, mn, d) > _native.NOALLOC_SCRATCH_BYTES
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    rc = built_lib.mps_apply_2q_batch_noalloc(stream, ctypes.c_void_p(jobs.data_ptr()), 4, mm, mn,
+    rc = built_lib.mps_apply_2q_batch_noalloc(stream, ctypes.c_void_p(jobs.data_ptr()), 8, mm, mn,
                                               d, ctypes.byref(_native.SvdParams()))
     assert rc == _native.MPS_ERR_WORKSPACE
     assert "scratch" in _native.last_error()
