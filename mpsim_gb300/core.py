@@ -14,9 +14,13 @@ Differences from the reference, all deliberate:
 * the per-gate norm history ``_norms`` (mpsim/core.py:1160-1161, marked
   "TODO: Remove ... only for convenience in benchmarking") is opt-in via
   ``track_norms=True``: it is a full O(n d chi^3) sweep after every gate;
-* ``apply`` runs consecutive two-qudit gates on disjoint adjacent pairs as
-  one batched launch -- exact, because each merged matrix depends only on its
-  own two sites;
+* two-qudit gates on adjacent pairs are deferred: ``apply_two_qudit_gate``
+  (and ``apply``, the shorthands, the swap chains of non-adjacent gates)
+  validates at once and queues the gate, and the queue runs as one batched
+  launch when a gate shares a site with a queued one or anything reads the
+  sites -- exact, because each merged matrix depends only on its own two
+  sites; a device error of a queued gate is raised by the call that runs the
+  queue;
 * ``get_node(s)`` return host copies (TensorNetwork-like nodes with the
   reference's initial axis order: physical axis first);
 * ``from_wavefunction`` returns the reference's state in the left-canonical
@@ -295,11 +299,48 @@ class MPS:
         # (jobs, max_m, max_n, sweeps, start_event, end_event).
         self.timing = None
         self._device = _require_cuda()
+        # Two-qudit gates on adjacent pairs wait here until a gate that shares
+        # a site, or any operation that reads or rewrites sites, needs them;
+        # then they run as one batched launch (see _sites).
+        self._pending = []
+        self._pending_sites = set()
         d = self._qudit_dimension
         init = torch.zeros((self._nqudits, 1, d, 1), dtype=torch.complex64)
         init[:, 0, 0, 0] = 1.0
         init = init.to(self._device)
-        self._sites = [init[i].clone() for i in range(self._nqudits)]
+        self._site_list = [init[i].clone() for i in range(self._nqudits)]
+
+    # -- deferred two-qudit gates ---------------------------------------------
+    # apply_two_qudit_gate validates at once (the reference's exceptions) and
+    # queues the gate; gates on disjoint adjacent pairs commute, so applying
+    # the queue as one batch gives exactly the result of applying them one by
+    # one, and gate-by-gate callers get the batched kernels.  Every access to
+    # _sites runs the queue first; only the queueing path itself (validity,
+    # kept-count planning for a pair no queued gate touches, one-qudit gates
+    # on such sites) and the flush read _site_list directly.  A device error of
+    # a queued gate (NaN, timeout) is raised by the call that flushes it.
+    @property
+    def _sites(self):
+        if self._pending:
+            self._flush()
+        return self._site_list
+
+    @_sites.setter
+    def _sites(self, value):
+        if self._pending:
+            self._flush()
+        self._site_list = value
+
+    def _flush(self) -> None:
+        """Runs the queued two-qudit gates as one batched launch."""
+        pending = self._pending
+        self._pending = []
+        self._pending_sites = set()
+        if pending:
+            self._run_pairs(pending)
+
+    def _touches_pending(self, *sites) -> bool:
+        return any(s in self._pending_sites for s in sites)
 
     # -- plumbing ----------------------------------------------------------
     @property
@@ -355,7 +396,8 @@ class MPS:
         return self._max_bond_dimensions
 
     def is_valid(self) -> bool:
-        s = self._sites
+        # queued gates keep every bond consistent, so the current list answers
+        s = self._site_list
         if len(s) < 2:
             return False
         d = self._qudit_dimension
@@ -690,7 +732,9 @@ class MPS:
         renorm = kwargs.get("renormalize_after_non_unitary") is not False
         ortho = kwargs.get("ortho_after_non_unitary") is not False
         norm = self.norm() if (not unitary and renorm) else None
-        site = self._sites[node_index]
+        if self._touches_pending(node_index):
+            self._flush()
+        site = self._site_list[node_index]
         g = self._to_device_gate(mat)
         _native.check(self._lib().mps_apply_1q(
             self._stream(), ctypes.c_void_p(site.data_ptr()), int(site.shape[0]),
@@ -776,7 +820,9 @@ class MPS:
             i, j = j, i
         lc = kwargs["keep_left_canonical"] if "keep_left_canonical" in kwargs else True
         maxsvals = parse_truncation(kwargs, self.max_bond_dimension_of, min(i, j))
-        a, b = self._sites[i], self._sites[j]
+        if self._touches_pending(i, j):
+            self._flush()
+        a, b = self._site_list[i], self._site_list[j]
         m = int(a.shape[0]) * d
         n = int(b.shape[2]) * d
         k = kept_count(maxsvals, min(m, n))
@@ -797,8 +843,9 @@ class MPS:
             original = i
             self.move_node_from_left_to_right(i, j - 1, **kwargs)
             i = j - 1
-        mat, left, k, lc = self._prepare_pair(g, i, j, kwargs)
-        self._run_pairs([(mat, left, k, lc)])
+        pair = self._prepare_pair(g, i, j, kwargs)      # flushes a queued gate on i or j
+        self._pending.append(pair)
+        self._pending_sites.update((pair[1], pair[1] + 1))
         if invert:
             self.move_node_from_right_to_left(i, original, **kwargs)
         if self.track_norms:
@@ -906,65 +953,38 @@ class MPS:
 
     # -- operation lists ---------------------------------------------------
     def apply(self, operations, **kwargs) -> None:
-        """Applies operations in order (core.py:1221-1276).
-
-        Consecutive two-qudit gates on disjoint adjacent pairs are gathered
-        into one batched launch; a one-qudit gate on a site with a pending
-        two-qudit gate (or any other operation that touches it) first
-        flushes the batch, so the result equals in-order application."""
+        """Applies operations in order (core.py:1221-1276), each through
+        apply_one_qudit_gate / apply_two_qudit_gate: two-qudit gates on
+        disjoint adjacent pairs join the state's queue and run as one batched
+        launch, so the result equals in-order application."""
         try:
             operations = iter(operations)
         except TypeError:
             operations = (operations,)
-        pending = []
-        busy = set()
-
-        def flush():
-            if pending:
-                self._run_pairs(pending)
-                pending.clear()
-                busy.clear()
-
-        batchable = not self.track_norms
         for op in operations:
             if not isinstance(op, MPSOperation):
-                flush()
                 raise TypeError("Argument operation should be of type MPSOperation but is "
                                 f"of type {type(op)}.")
             if not op.is_valid():
-                flush()
                 raise ValueError("Input MPS Operation is not valid.")
             if op.is_single_qudit_operation():
                 (i,) = op.qudit_indices
-                if i in busy:
-                    flush()
                 self.apply_one_qudit_gate(op.node(copy=False), i, **kwargs)
             elif op.is_two_qudit_operation():
                 i, j = op.qudit_indices
-                adjacent = (isinstance(i, (int, np.integer)) and isinstance(j, (int, np.integer))
-                            and abs(int(i) - int(j)) == 1 and 0 <= min(i, j)
-                            and max(i, j) < self._nqudits)
-                if batchable and adjacent:
-                    if i in busy or j in busy:
-                        flush()
-                    pending.append(self._prepare_pair(op.node(copy=False), int(i), int(j), kwargs))
-                    busy.update((int(i), int(j)))
-                else:
-                    flush()
-                    self.apply_two_qudit_gate(op.node(copy=False), i, j, **kwargs)
+                self.apply_two_qudit_gate(op.node(copy=False), i, j, **kwargs)
             else:
-                flush()
                 raise ValueError(
                     "Only one-qudit and two-qudit gates are supported. To apply a gate on three or "
                     "more qudits, the gate must be compiled into a sequence of one- and two-qudit "
                     "gates.")
-        flush()
 
     def apply_layer(self, one_qudit: Optional[np.ndarray], pair_left: Sequence[int],
                     two_qudit: Optional[np.ndarray], **kwargs) -> None:
         """One brickwork layer: ``one_qudit[i]`` (d x d) on every site i, then
         ``two_qudit[p]`` (d^2 x d^2) on (pair_left[p], pair_left[p] + 1), the
         pairs disjoint -- the same result as applying the gates one by one."""
+        self._flush()
         if one_qudit is not None:
             self._apply_one_qudit_layer(one_qudit)
         if two_qudit is None or len(pair_left) == 0:
@@ -992,6 +1012,7 @@ class MPS:
         """``apply_layer`` for gates already on the device (torch complex64:
         one_qudit_dev (n, d, d), two_qudit_dev (p, d^2, d^2)).  Skips the
         host-side unitarity and edge checks; shapes are still validated."""
+        self._flush()
         d = self._qudit_dimension
         if one_qudit_dev is not None:
             if tuple(one_qudit_dev.shape) != (self._nqudits, d, d):
@@ -1071,9 +1092,12 @@ class MPS:
         return self.__copy__()
 
     def __copy__(self):
+        sites = self._sites                   # runs queued gates first
         new = MPS.__new__(MPS)
         new.__dict__.update(self.__dict__)
-        new._sites = [t.clone() for t in self._sites]
+        new._pending = []
+        new._pending_sites = set()
+        new._site_list = [t.clone() for t in sites]
         new._norms = list(self._norms)
         new.svals_history = list(self.svals_history)
         new.svd_params = _native.SvdParams(self.svd_params.max_sweeps, self.svd_params.tol, 0, 0,
