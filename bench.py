@@ -345,7 +345,8 @@ def main():
     import __graft_entry__ as ge
     from mpsim_gb300 import circuits as C
     from mpsim_gb300 import _native
-    from mpsim_gb300.core import MPS
+    from mpsim_gb300.core import MPS, MPSOperation
+    from mpsim_gb300.gates import Node
 
     ge.build()
     torch.cuda.set_device(local)
@@ -383,6 +384,21 @@ def main():
         mps = MPS(circ.nqudits, d)
         for one, left, two in host_layers:
             mps.apply_layer(one, left, two, maxsvals=maxs)
+        return mps.norm()
+
+    # the reference's own call: MPS.apply with a list of MPSOperation per layer
+    host_ops = []
+    for one, left, two in host_layers:
+        ops = [MPSOperation(Node(one[i]), i) for i in range(circ.nqudits)]
+        ops += [MPSOperation(Node(two[p].reshape((d,) * 4)), (int(i), int(i) + 1))
+                for p, i in enumerate(left)]
+        host_ops.append(ops)
+
+    def step_apply_ops():
+        flush.fill_(1)
+        mps = MPS(circ.nqudits, d)
+        for ops in host_ops:
+            mps.apply(ops, maxsvals=maxs)
         return mps.norm()
 
     def barrier():
@@ -447,6 +463,18 @@ def main():
     e2e_ms = max_over_ranks(e0.elapsed_time(e1))
     e2e_value = whole_job_rate(ngates, args.steps, world, e2e_ms)
 
+    step_apply_ops()
+    barrier()
+    a0 = torch.cuda.Event(enable_timing=True)
+    a1 = torch.cuda.Event(enable_timing=True)
+    a0.record()
+    for _ in range(args.steps):
+        step_apply_ops()
+    a1.record()
+    barrier()
+    ops_ms = max_over_ranks(a0.elapsed_time(a1))
+    ops_value = whole_job_rate(ngates, args.steps, world, ops_ms)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, dt, norm_cost, n2, n1 = cpu_sample(circ)
@@ -477,7 +505,10 @@ def main():
                          "mean_sweeps": mean_sweeps,
                          "fp32_simt_nominal_frac": (achieved / 80.5) if achieved else None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": 8},
+                    "d2h_bytes_per_step": 8, "call": "MPS.apply_layer per layer, pinned host gates"},
+            "e2e_reference_api": {"value": ops_value, "unit": UNIT,
+                                  "call": "MPS.apply([MPSOperation, ...], maxsvals=256) per layer, "
+                                          "host gates, norm read back"},
             "gpu_launches": int(launches),
             "clocks": clk,
             "final_norm": float(norms[-1]) if norms else None,

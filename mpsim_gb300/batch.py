@@ -147,6 +147,7 @@ class MPSBatch:
         for c, i, a_out, b_out in outs:
             self.states[c]._sites[i] = a_out
             self.states[c]._sites[i + 1] = b_out
+            self.states[c]._version += 1
 
 
 def run_circuits(circuits, device=None) -> List[MPS]:

@@ -19,8 +19,8 @@ Differences from the reference, all deliberate:
   validates at once and queues the gate, and the queue runs as one batched
   launch when a gate shares a site with a queued one or anything reads the
   sites -- exact, because each merged matrix depends only on its own two
-  sites; a device error of a queued gate is raised by the call that runs the
-  queue;
+  sites; unitary one-qudit gates are queued too and launched together; a
+  device error of a queued gate is raised by the call that runs the queue;
 * ``get_node(s)`` return host copies (TensorNetwork-like nodes with the
   reference's initial axis order: physical axis first);
 * ``from_wavefunction`` returns the reference's state in the left-canonical
@@ -304,6 +304,11 @@ class MPS:
         # then they run as one batched launch (see _sites).
         self._pending = []
         self._pending_sites = set()
+        self._pending_1q = []            # (site, d x d complex64 gate) waiting for one launch
+        self._pending_1q_sites = set()
+        # bumped whenever a site tensor is replaced; is_valid caches per value
+        self._version = 0
+        self._valid_at = (-1, False)
         d = self._qudit_dimension
         init = torch.zeros((self._nqudits, 1, d, 1), dtype=torch.complex64)
         init[:, 0, 0, 0] = 1.0
@@ -319,28 +324,57 @@ class MPS:
     # kept-count planning for a pair no queued gate touches, one-qudit gates
     # on such sites) and the flush read _site_list directly.  A device error of
     # a queued gate (NaN, timeout) is raised by the call that flushes it.
+    # Unitary one-qudit gates are queued the same way and launched together
+    # (one copy of all their matrices, one mps_apply_1q_batch): they touch no
+    # site a queued two-qudit gate touches, and at most one gate per site is
+    # queued, so the order of launch among them is free.
     @property
     def _sites(self):
-        if self._pending:
+        if self._pending or self._pending_1q:
             self._flush()
         return self._site_list
 
     @_sites.setter
     def _sites(self, value):
-        if self._pending:
+        if self._pending or self._pending_1q:
             self._flush()
         self._site_list = value
+        self._version += 1
 
     def _flush(self) -> None:
-        """Runs the queued two-qudit gates as one batched launch."""
+        """Runs the queued one-qudit gates, then the queued two-qudit gates
+        (disjoint sites), each queue as one batched launch."""
+        self._flush_1q()
         pending = self._pending
         self._pending = []
         self._pending_sites = set()
         if pending:
             self._run_pairs(pending)
 
+    def _flush_1q(self) -> None:
+        pending = self._pending_1q
+        if not pending:
+            return
+        self._pending_1q = []
+        self._pending_1q_sites = set()
+        d, n1 = self._qudit_dimension, len(pending)
+        mats = np.ascontiguousarray(np.stack([m for _, m in pending]).astype(np.complex64))
+        g = torch.from_numpy(mats).to(self._device)
+        table = np.zeros(n1, dtype=_native.JOB1_DTYPE)
+        for q, (i, _) in enumerate(pending):
+            site = self._site_list[i]
+            table[q]["site"] = site.data_ptr()
+            table[q]["gate"] = g[q].data_ptr()
+            table[q]["chi_l"], table[q]["chi_r"] = int(site.shape[0]), int(site.shape[2])
+        jt = torch.from_numpy(table.view(np.uint8)).to(self._device)
+        _native.check(self._lib().mps_apply_1q_batch(self._stream(), ctypes.c_void_p(jt.data_ptr()),
+                                                     n1, d))
+
     def _touches_pending(self, *sites) -> bool:
         return any(s in self._pending_sites for s in sites)
+
+    def _touches_pending_1q(self, *sites) -> bool:
+        return any(s in self._pending_1q_sites for s in sites)
 
     # -- plumbing ----------------------------------------------------------
     @property
@@ -396,7 +430,15 @@ class MPS:
         return self._max_bond_dimensions
 
     def is_valid(self) -> bool:
-        # queued gates keep every bond consistent, so the current list answers
+        # queued gates keep every bond consistent, so the current list answers;
+        # the answer only changes when a site tensor is replaced (_version)
+        if self._valid_at[0] == self._version:
+            return self._valid_at[1]
+        ok = self._check_valid()
+        self._valid_at = (self._version, ok)
+        return ok
+
+    def _check_valid(self) -> bool:
         s = self._site_list
         if len(s) < 2:
             return False
@@ -686,6 +728,7 @@ class MPS:
         self._sites[i] = left[:, :keep].reshape(cl, d, keep) if keep == r else \
             left[:, :keep].contiguous().reshape(cl, d, keep)
         self._sites[i + 1] = new_next
+        self._version += 1
 
     def orthonormalize_left_edge_of(self, node_index: int, threshold: float = 1e-8) -> None:
         """SVD of site i with columns (digit, right bond): site i <- V^H,
@@ -707,6 +750,7 @@ class MPS:
                left, 0, r, 1, 0, new_prev, 0, keep, 1)
         self._sites[i] = right[:keep].reshape(keep, d, cr)
         self._sites[i - 1] = new_prev
+        self._version += 1
 
     # -- one-qudit gates ---------------------------------------------------
     def _check_one_qudit(self, gate, node_index):
@@ -729,10 +773,18 @@ class MPS:
         self._check_one_qudit(gate, node_index)
         mat = gate_tensor(gate)
         unitary = is_unitary(np.asarray(mat))
+        if unitary:
+            # queued (see _flush_1q); a queued gate on the same site runs first
+            if self._touches_pending(node_index) or self._touches_pending_1q(node_index):
+                self._flush()
+            # a copy: the caller may reuse its array before the queue runs
+            self._pending_1q.append((node_index, np.array(mat, dtype=np.complex64)))
+            self._pending_1q_sites.add(node_index)
+            return
         renorm = kwargs.get("renormalize_after_non_unitary") is not False
         ortho = kwargs.get("ortho_after_non_unitary") is not False
         norm = self.norm() if (not unitary and renorm) else None
-        if self._touches_pending(node_index):
+        if self._touches_pending(node_index) or self._pending_1q:
             self._flush()
         site = self._site_list[node_index]
         g = self._to_device_gate(mat)
@@ -822,6 +874,8 @@ class MPS:
         maxsvals = parse_truncation(kwargs, self.max_bond_dimension_of, min(i, j))
         if self._touches_pending(i, j):
             self._flush()
+        elif self._touches_pending_1q(i, j):
+            self._flush_1q()              # those one-qudit gates come first
         a, b = self._site_list[i], self._site_list[j]
         m = int(a.shape[0]) * d
         n = int(b.shape[2]) * d
@@ -916,6 +970,7 @@ class MPS:
             raise _native.NativeError(rc, _native.last_error())
         for left, a_out, b_out in outs:
             self._sites[left] = a_out
+            self._version += 1
             self._sites[left + 1] = b_out
         if rec:
             sv = svals.cpu().numpy()
@@ -1097,6 +1152,8 @@ class MPS:
         new.__dict__.update(self.__dict__)
         new._pending = []
         new._pending_sites = set()
+        new._pending_1q = []
+        new._pending_1q_sites = set()
         new._site_list = [t.clone() for t in sites]
         new._norms = list(self._norms)
         new.svals_history = list(self.svals_history)

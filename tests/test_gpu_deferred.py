@@ -92,3 +92,33 @@ def test_apply_operations_and_nonadjacent(cuda):
         m.cnot(0, i)
     psi = m.wavefunction()
     assert abs(abs(psi[0]) - 2 ** -0.5) < 1e-6 and abs(abs(psi[-1]) - 2 ** -0.5) < 1e-6
+
+
+def test_one_qudit_gates_are_queued_and_ordered(cuda):
+    rng = np.random.default_rng(3)
+    u = [G.haar_random_matrix(1, 2, 40 + i) for i in range(6)]
+    w, _ = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))
+    a = MPS(6)
+    for i in range(6):
+        a.apply_one_qudit_gate(u[i], i)
+    assert len(a._pending_1q) == 6            # one launch for all six
+    mine = w.copy()
+    a.apply_one_qudit_gate(mine, 5)            # site 5 is queued: the six run first
+    assert len(a._pending_1q) == 1
+    mine[:] = 0                                # reusing the array must not change the queued gate
+    a.cnot(2, 3)                               # queued beside the gate on 5
+    a.apply_one_qudit_gate(u[0], 2)            # site 2 waits for the cnot
+    psi = a.wavefunction()
+    state = np.zeros(2 ** 6, complex)
+    state[0] = 1
+    state = state.reshape((2,) * 6)
+
+    def one(st, g, q):
+        return np.moveaxis(np.tensordot(g, st, axes=([1], [q])), 0, q)
+    for i in range(6):
+        state = one(state, u[i], i)
+    state = one(state, w, 5)
+    cn = np.asarray(G.cnot().tensor).reshape(2, 2, 2, 2)
+    state = np.moveaxis(np.tensordot(cn, state, axes=([2, 3], [2, 3])), [0, 1], [2, 3])
+    state = one(state, u[0], 2)
+    assert np.allclose(psi, state.reshape(-1), atol=2e-6)
