@@ -192,14 +192,15 @@ __device__ __forceinline__ void publish_offmax(float offmax, float* s_off, int n
 // Loads of X and V use __ldcg (L2, bypassing L1): inside the persistent
 // sweep kernel another CTA may have rewritten a column since this SM last
 // cached it.
+// Returns whether any pair rotated (the same on every thread).
 template <int BC, int ROWS>
-__device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, const TwoQGeom& g,
+__device__ __forceinline__ bool visit_full(const mps_2q_job* __restrict__ jobs, const TwoQGeom& g,
                                            int j, int round, int pair, float tol2, float2* smem,
                                            float* s_off) {
-    if (g.done[j]) return;
+    if (g.done[j]) return false;
     const JobShape sh = job_shape<BC>(jobs, j, g.d);
-    if (sh.C < 2) return;
-    if (round >= sh.nb - 1 || pair >= sh.nb / 2) return;
+    if (sh.C < 2) return false;
+    if (round >= sh.nb - 1 || pair >= sh.nb / 2) return false;
     int I, J;
     tournament_pair(sh.nb, round, pair, I, J);
     const int Lw = (sh.L + 31) & ~31;
@@ -227,6 +228,7 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
     __syncthreads();
 
     float offmax = 0.f;
+    bool rotated = false;
     for (int step = 0; step < W - 1; ++step) {
         int p, q;
         tournament_pair(W, step, warp, p, q);
@@ -263,6 +265,7 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
             }
             na = warp_sum(na);
             nq = warp_sum(nq);
+            rotated = true;
             if (sh.track_v && lane < W) {
                 cf qa = Qs[p * W + lane], qb = Qs[q * W + lane];
                 apply_rot(R, qa, qb);
@@ -277,14 +280,18 @@ __device__ __forceinline__ void visit_full(const mps_2q_job* __restrict__ jobs, 
         }
         __syncthreads();
     }
+    const bool any = __syncthreads_or(rotated ? 1 : 0) != 0;
     for (int c = warp; c < W; c += BC) {
         const int pc = phys_col(g, j, block_col(c, I, J, BC));
-        cf* dst = X + (size_t)pc * g.lslot;
-        for (int r = lane; r < Lw; r += 32) dst[r] = Xs[(size_t)c * Lw + r];
+        if (any) {
+            cf* dst = X + (size_t)pc * g.lslot;
+            for (int r = lane; r < Lw; r += 32) dst[r] = Xs[(size_t)c * Lw + r];
+        }
         if (lane == 0) g.cnrm[(size_t)j * g.cslot + pc] = nrm[c];
     }
-    if (sh.track_v) update_v<BC>(g, j, sh.C, I, J, Qs);
+    if (sh.track_v && any) update_v<BC>(g, j, sh.C, I, J, Qs);
     publish_offmax(offmax, s_off, BC, g.offmax + j);
+    return any;
 }
 
 template <int BC, int ROWS>
@@ -442,14 +449,14 @@ constexpr int kHandoffTries = 1 << 18;
 constexpr unsigned kHandoffSuspendNs = 1000;
 
 template <int BC, int ROWS>
-__device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict__ jobs,
+__device__ __forceinline__ bool visit_ring_handoff(const mps_2q_job* __restrict__ jobs,
                                                    const TwoQGeom& g, int j, int round, int pair,
                                                    float tol2, float2* smem, float* s_off,
                                                    uint64_t* bars, unsigned& parity, int* err) {
-    if (g.done[j]) return;
+    if (g.done[j]) return false;
     const JobShape sh = job_shape<BC>(jobs, j, g.d);
-    if (sh.C < 2) return;
-    if (round >= sh.nb - 1 || pair >= sh.nb / 2) return;
+    if (sh.C < 2) return false;
+    if (round >= sh.nb - 1 || pair >= sh.nb / 2) return false;
     int I, J;
     tournament_pair(sh.nb, round, pair, I, J);
     constexpr int LW = 32 * ROWS;
@@ -565,6 +572,7 @@ __device__ __forceinline__ void visit_ring_handoff(const mps_2q_job* __restrict_
     }
     if (sh.track_v && any) update_v<BC>(g, j, sh.C, I, J, Qs);
     publish_offmax(offmax, s_off, BC, g.offmax + j);
+    return any;
 }
 
 template <int BC, int ROWS>
@@ -584,13 +592,21 @@ ring_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, fl
 // no deadlock, whatever number of CTAs is resident.  The wait polls a flag
 // at most wait_limit times (with __nanosleep backoff); on expiry it raises
 // the error flag and the CTA leaves, as do the others once they see it.
+//
+// A visit is skipped when it would rotate nothing for certain: its last run
+// (the same round and pair in an earlier sweep, at time qstamp) rotated
+// nothing, and neither block has changed since (vstamp older than qstamp:
+// no visit rotated it and the per-sweep sort kept its set of columns).  Its
+// pairs then hold the same bits that were checked, so the visit would find
+// every one below the threshold again.  A skipped item still waits for its
+// blocks and publishes its round.  tbase = sweep * (rounds + 1).
 template <int BC, int ROWS>
 __global__ void __launch_bounds__(BC * 32)
 sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int njobs, int rounds,
-             int pairs, SweepSync sync) {
+             int pairs, SweepSync sync, int tbase) {
     extern __shared__ float2 smem[];
     __shared__ float s_off[BC];
-    __shared__ int s_item, s_abort;
+    __shared__ int s_item, s_abort, s_skip;
     // ring hand-off barriers, one per (step < BC-1, visitor); see
     // visit_ring_handoff
     __shared__ __align__(8) uint64_t s_bar[(BC - 1) * BC];
@@ -617,32 +633,49 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
             active = sh.C >= 2 && r < sh.nb - 1 && p < sh.nb / 2;
             if (active) tournament_pair(sh.nb, r, p, I, J);
         }
-        if (active && r > 0) {
+        if (active) {
+            volatile int* vst = g.vstamp + (size_t)j * g.nbmax;
+            volatile int* qst = g.qstamp + (size_t)j * g.qstride + r * pairs + p;
             if (threadIdx.x == 0) {
-                volatile int* fl = sync.block_round + (size_t)j * sync.nbmax;
-                volatile int* err = sync.error;
-                // the test hook waits for a round no block ever reaches
-                const int need = (sync.stall_test && item == per_round) ? rounds + 1 : r - 1;
-                int polls = 0;
-                while ((fl[I] < need || fl[J] < need) && *err == 0) {
-                    if (++polls > sync.wait_limit) {
-                        atomicExch(sync.error, 1);
-                        break;
+                if (r > 0) {
+                    volatile int* fl = sync.block_round + (size_t)j * sync.nbmax;
+                    volatile int* err = sync.error;
+                    // the test hook waits for a round no block ever reaches
+                    const int need = (sync.stall_test && item == per_round) ? rounds + 1 : r - 1;
+                    int polls = 0;
+                    while ((fl[I] < need || fl[J] < need) && *err == 0) {
+                        if (++polls > sync.wait_limit) {
+                            atomicExch(sync.error, 1);
+                            break;
+                        }
+                        __nanosleep(64);
                     }
-                    __nanosleep(64);
+                    s_abort = *err;
+                    __threadfence();
                 }
-                s_abort = *err;
-                __threadfence();
+                const int q = *qst;
+                s_skip = (q >= 0 && q > vst[I] && q > vst[J]) ? 1 : 0;
             }
             __syncthreads();
             if (s_abort) return;
-        }
-        if (active) {
-            if (r == 0) visit_full<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off);
-            else visit_ring_handoff<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off, s_bar, parity,
-                                              sync.error);
+            const bool skip = s_skip != 0;
+            bool rot = false;
+            if (!skip) {
+                if (r == 0) rot = visit_full<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off);
+                else rot = visit_ring_handoff<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off, s_bar,
+                                                        parity, sync.error);
+            }
             __syncthreads();
             if (threadIdx.x == 0) {
+                if (!skip) {
+                    const int now = tbase + r + 1;
+                    if (rot) {
+                        vst[I] = now;
+                        vst[J] = now;
+                    } else {
+                        *qst = now;
+                    }
+                }
                 __threadfence();
                 atomicExch(sync.block_round + (size_t)j * sync.nbmax + I, r);
                 atomicExch(sync.block_round + (size_t)j * sync.nbmax + J, r);
@@ -699,7 +732,7 @@ __global__ void init_slots_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom 
 constexpr int PRESORT_T = 512;
 
 __global__ void __launch_bounds__(PRESORT_T)
-presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2) {
+presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2, int bc, int tpre) {
     extern __shared__ float2 sm1[];
     float* key = reinterpret_cast<float*>(sm1);
     int* idx = reinterpret_cast<int*>(key + npow2);
@@ -736,6 +769,21 @@ presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2) {
                 }
             }
             __syncthreads();
+        }
+    }
+    if (g.vstamp) {
+        // a block whose set of columns changes counts as changed (its pairs
+        // are not the ones last checked); moves inside a block do not
+        int* oldpos = reinterpret_cast<int*>(key);     // the keys are no longer needed
+        for (int i = tid; i < C; i += PRESORT_T) oldpos[__ldcg(g.cmap + (size_t)j * g.cslot + i)] = i;
+        __syncthreads();
+        int* vst = g.vstamp + (size_t)j * g.nbmax;
+        for (int c = tid; c < C; c += PRESORT_T) {
+            const int ob = oldpos[idx[c]] / bc, nb = c / bc;
+            if (ob != nb) {
+                vst[ob] = tpre;
+                vst[nb] = tpre;
+            }
         }
     }
     for (int i = tid; i < C; i += PRESORT_T) g.cmap[(size_t)j * g.cslot + i] = idx[i];
@@ -1272,7 +1320,7 @@ int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g
 
 template <int BC, int ROWS>
 int launch_sweep(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const TwoQGeom& g,
-                 float tol2, int lw, const SweepSync& sync, cudaStream_t s) {
+                 float tol2, int lw, const SweepSync& sync, int tbase, cudaStream_t s) {
     static std::once_flag once;
     static int limit = 0, rc = MPS_OK, ctas = 0;
     if (prepare_kernel(sweep_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
@@ -1289,13 +1337,14 @@ int launch_sweep(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const
     const int items = rounds * njobs * pairs;
     const int grid = items < ctas ? items : ctas;
     if (grid <= 0) return MPS_OK;
-    sweep_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, tol2, njobs, rounds, pairs, sync);
+    sweep_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, tol2, njobs, rounds, pairs, sync,
+                                                       tbase);
     MPS_LAUNCH_CHECK("sweep_kernel");
     return MPS_OK;
 }
 
 typedef int (*sweep_fn)(const mps_2q_job*, int, int, int, const TwoQGeom&, float, int,
-                        const SweepSync&, cudaStream_t);
+                        const SweepSync&, int, cudaStream_t);
 
 sweep_fn pick_sweep(int lw) {
     if (lw <= 576) {
@@ -1329,8 +1378,8 @@ visit_fn pick_visit(int lw, int* bc) {
 struct Layout {
     int lslot, cslot;
     size_t off_X, off_V, off_T, off_sig, off_perm, off_cmap, off_cnrm, off_off, off_done, off_need,
-        off_counter, off_scale, off_nrm2, off_sync, total;
-    int nbmax;
+        off_counter, off_scale, off_nrm2, off_sync, off_vst, off_qst, total;
+    int nbmax, qstride;
 };
 
 // Column length of a slot: the ring kernel reads exactly 32*ROWS rows, so
@@ -1366,6 +1415,10 @@ Layout make_layout(int njobs, int max_m, int max_n) {
     // for the smallest block width, 8 columns)
     lo.nbmax = (int)align_up((size_t)(lo.cslot + 7) / 8, 2);
     lo.off_sync = o; o = align_up(o + (2 + nj * lo.nbmax) * sizeof(int), 256);
+    // visit skipping: a stamp per column block and per (round, pair)
+    lo.qstride = lo.nbmax * (lo.nbmax / 2);
+    lo.off_vst = o; o = align_up(o + nj * lo.nbmax * sizeof(int), 256);
+    lo.off_qst = o; o = align_up(o + nj * lo.qstride * sizeof(int), 256);
     lo.total = o;
     return lo;
 }
@@ -1420,6 +1473,10 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     g.cnrm = reinterpret_cast<float*>(ws + lo.off_cnrm);
     g.scale = reinterpret_cast<int*>(ws + lo.off_scale);
     g.nrm2 = reinterpret_cast<double*>(ws + lo.off_nrm2);
+    g.vstamp = reinterpret_cast<int*>(ws + lo.off_vst);
+    g.qstamp = reinterpret_cast<int*>(ws + lo.off_qst);
+    g.nbmax = lo.nbmax;
+    g.qstride = lo.qstride;
 
     int max_sweeps = 40;
     float tol = 0.f;
@@ -1448,8 +1505,10 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     sync.wait_limit = (params && params->wait_limit > 0) ? params->wait_limit : (1 << 22);
     sync.stall_test = params ? params->stall_test : 0;
 
-    // padding rows and columns of X must be zero
+    // padding rows and columns of X must be zero; no block has a stamp yet
     MPS_CUDA_CHECK(cudaMemsetAsync(g.X, 0, lo.off_V - lo.off_X, s));
+    MPS_CUDA_CHECK(cudaMemsetAsync(g.vstamp, 0xff, lo.off_qst - lo.off_vst +
+                                                       (size_t)njobs * lo.qstride * sizeof(int), s));
     {
         const size_t total = (size_t)njobs * lo.cslot * lo.cslot;
         int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
@@ -1482,14 +1541,15 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
             MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
             if (cmax > 2 * bc) {
-                presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2);
+                presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc,
+                                                                   sweeps * (rounds + 1));
                 MPS_LAUNCH_CHECK("presort_kernel");
             }
             // one persistent launch runs every round of the sweep
             MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, 2 * sizeof(int), s));
             MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
                                            (size_t)njobs * lo.nbmax * sizeof(int), s));
-            rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, s);
+            rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, sweeps * (rounds + 1), s);
             if (rc) return rc;
             sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
@@ -1645,6 +1705,11 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     g.cnrm = reinterpret_cast<float*>(ws + lo.off_cnrm);
     g.scale = reinterpret_cast<int*>(ws + lo.off_scale);
     g.nrm2 = reinterpret_cast<double*>(ws + lo.off_nrm2);
+    // the per-round visit kernels of this entry point do not skip visits
+    g.vstamp = nullptr;
+    g.qstamp = nullptr;
+    g.nbmax = lo.nbmax;
+    g.qstride = lo.qstride;
 
     int max_sweeps = 40;
     float tol = 0.f;
@@ -1691,7 +1756,7 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
         for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
             MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
             if (cmax > 2 * bc) {
-                presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2);
+                presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc, 0);
                 MPS_LAUNCH_CHECK("presort_kernel");
             }
             for (int r = 0; r < rounds; ++r) {

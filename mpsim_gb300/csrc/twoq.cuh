@@ -32,6 +32,12 @@ struct TwoQGeom {
     float* cnrm;      // njobs * cslot: squared norm of each physical column
     int* scale;       // njobs: theta was multiplied by 2^scale[j] before the SVD
     double* nrm2;     // njobs: |theta|_F^2 (scratch of the scaling)
+    // Visit skipping of the sweep kernel (null where unused).  Times count
+    // t = sweep * (rounds + 1) + round + 1, and sweep * (rounds + 1) for the
+    // sort before a sweep.
+    int* vstamp;      // njobs * nbmax: last time a column block changed
+    int* qstamp;      // njobs * qstride: last time visit (round, pair) rotated nothing
+    int nbmax, qstride;
 };
 
 // Work distribution of the persistent sweep kernel.
