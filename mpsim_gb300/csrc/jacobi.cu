@@ -634,9 +634,16 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
             if (active) tournament_pair(sh.nb, r, p, I, J);
         }
         if (active) {
+            // a job of one block pair has one visit per sweep, and a visit
+            // that rotates nothing ends it: no stamps (and r > 0 implies nb > 2)
+            const bool track = nb > 2;
             volatile int* vst = g.vstamp + (size_t)j * g.nbmax;
             volatile int* qst = g.qstamp + (size_t)j * g.qstride + r * pairs + p;
-            if (threadIdx.x == 0) {
+            if (track && threadIdx.x == 0) {
+                // qstamp of this (round, pair) changes only when this item
+                // runs, so it is read before the wait; the block stamps only
+                // after it, and only when the visit was once quiet
+                const int q = *qst;
                 if (r > 0) {
                     volatile int* fl = sync.block_round + (size_t)j * sync.nbmax;
                     volatile int* err = sync.error;
@@ -653,12 +660,13 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
                     s_abort = *err;
                     __threadfence();
                 }
-                const int q = *qst;
                 s_skip = (q >= 0 && q > vst[I] && q > vst[J]) ? 1 : 0;
             }
-            __syncthreads();
-            if (s_abort) return;
-            const bool skip = s_skip != 0;
+            if (track) {
+                __syncthreads();
+                if (s_abort) return;
+            }
+            const bool skip = track && s_skip != 0;
             bool rot = false;
             if (!skip) {
                 if (r == 0) rot = visit_full<BC, ROWS>(jobs, g, j, r, p, tol2, smem, s_off);
@@ -667,7 +675,7 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
             }
             __syncthreads();
             if (threadIdx.x == 0) {
-                if (!skip) {
+                if (track && !skip) {
                     const int now = tbase + r + 1;
                     if (rot) {
                         vst[I] = now;
