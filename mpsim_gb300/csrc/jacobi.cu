@@ -426,6 +426,22 @@ __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, 
     publish_offmax(offmax, s_off, BC, g.offmax + j);
 }
 
+// Two adjacent rows (2k, 2k+1) of a column as one 16-byte access: global
+// through L2 only (another CTA may have rewritten the column), or shared.
+__device__ __forceinline__ void ld_pair(const cf* col, int k, cf& a, cf& b) {
+    const float4 t = __ldcg(reinterpret_cast<const float4*>(col) + k);
+    a = cmake(t.x, t.y);
+    b = cmake(t.z, t.w);
+}
+__device__ __forceinline__ void lds_pair(const cf* col, int k, cf& a, cf& b) {
+    const float4 t = reinterpret_cast<const float4*>(col)[k];
+    a = cmake(t.x, t.y);
+    b = cmake(t.z, t.w);
+}
+__device__ __forceinline__ void st_pair(cf* col, int k, cf a, cf b) {
+    reinterpret_cast<float4*>(col)[k] = make_float4(a.x, a.y, b.x, b.y);
+}
+
 // The same BC*BC pairs for the persistent sweep kernel, with the J columns
 // kept in shared memory instead of travelling warp to warp: at step s warp w
 // takes visitor (w - s) mod BC (the order of visit_ring), so visitor v passes
@@ -476,10 +492,13 @@ __device__ __forceinline__ bool visit_ring_handoff(const mps_2q_job* __restrict_
         cf* vd = vis + (size_t)warp * LW;
         float vn = 0.f;
 #pragma unroll
+        for (int i = 0; i < ROWS / 2; ++i) {
+            ld_pair(hs, lane + 32 * i, hx[2 * i], hx[2 * i + 1]);
+            ld_pair(vs, lane + 32 * i, vx[2 * i], vx[2 * i + 1]);
+            st_pair(vd, lane + 32 * i, vx[2 * i], vx[2 * i + 1]);
+        }
+#pragma unroll
         for (int i = 0; i < ROWS; ++i) {
-            hx[i] = __ldcg(hs + lane + 32 * i);
-            vx[i] = __ldcg(vs + lane + 32 * i);
-            vd[lane + 32 * i] = vx[i];
             hn += cabs2(hx[i]);
             vn += cabs2(vx[i]);
         }
@@ -506,7 +525,7 @@ __device__ __forceinline__ bool visit_ring_handoff(const mps_2q_job* __restrict_
                 if (++tries > kHandoffTries) expired = true;
             }
 #pragma unroll
-            for (int i = 0; i < ROWS; ++i) vx[i] = vcol[lane + 32 * i];
+            for (int i = 0; i < ROWS / 2; ++i) lds_pair(vcol, lane + 32 * i, vx[2 * i], vx[2 * i + 1]);
         }
         const float vn = visn[v];
         cf gam = cmake(0.f, 0.f);
@@ -520,10 +539,9 @@ __device__ __forceinline__ bool visit_ring_handoff(const mps_2q_job* __restrict_
         if (r2 > tol2) {                        // warp-uniform (butterfly sums)
             const Rot R = make_rot(hn, vn, gam, g2);
 #pragma unroll
-            for (int i = 0; i < ROWS; ++i) {
-                apply_rot(R, hx[i], vx[i]);
-                vcol[lane + 32 * i] = vx[i];
-            }
+            for (int i = 0; i < ROWS; ++i) apply_rot(R, hx[i], vx[i]);
+#pragma unroll
+            for (int i = 0; i < ROWS / 2; ++i) st_pair(vcol, lane + 32 * i, vx[2 * i], vx[2 * i + 1]);
             // closed-form norm update, recomputed on cancellation (as in
             // visit_ring)
             const float dn = R.dn;
@@ -561,9 +579,10 @@ __device__ __forceinline__ bool visit_ring_handoff(const mps_2q_job* __restrict_
         cf* vd = X + (size_t)pv * g.lslot;
         const cf* vsrc = vis + (size_t)warp * LW;
 #pragma unroll
-        for (int i = 0; i < ROWS; ++i) {
-            hd[lane + 32 * i] = hx[i];
-            vd[lane + 32 * i] = vsrc[lane + 32 * i];
+        for (int i = 0; i < ROWS / 2; ++i) {
+            st_pair(hd, lane + 32 * i, hx[2 * i], hx[2 * i + 1]);
+            reinterpret_cast<float4*>(vd)[lane + 32 * i] =
+                reinterpret_cast<const float4*>(vsrc)[lane + 32 * i];
         }
     }
     if (lane == 0) {       // the norms the next sweep's sort reads
