@@ -57,12 +57,20 @@ namespace {
 // Squared cosine of the angle between two columns, |gamma|^2 / (a b).  A pair
 // rotates when it exceeds tol^2, and the per-job maximum of the same value
 // decides convergence, so a sweep that rotates nothing always ends the job.
-// Zero columns give 0; norms below the smallest normal float take IEEE
-// divisions (the fast ones flush them).
-__device__ __forceinline__ float pair_cos2(float g2, float a, float b) {
+// Zero columns give 0; when g2 = |gamma|^2 or a norm is below the smallest
+// normal float, the cosine is formed from |gamma| and the square roots of the
+// norms with IEEE operations instead.
+__device__ __forceinline__ float pair_cos2(cf gam, float g2, float a, float b) {
     const float kMinNormal = 1.17549435e-38f;
-    if (a >= kMinNormal && b >= kMinNormal) return __fdividef(__fdividef(g2, a), b);
-    return (a > 0.f && b > 0.f) ? (g2 / a) / b : 0.f;
+    if (g2 >= kMinNormal && a >= kMinNormal && b >= kMinNormal)
+        return __fdividef(__fdividef(g2, a), b);
+    // |gamma|^2 underflows once the columns are below ~1e-10 in norm (graded
+    // columns, as the L factor has from the start): take |gamma| itself.
+    // Pairs with a + b below 1e-36 leave no room for the rotation's
+    // 1/(a+b) and count as orthogonal.
+    if (!(a > 0.f && b > 0.f) || !(a + b >= 1e-36f)) return 0.f;
+    const float r = (hypotf(gam.x, gam.y) / sqrtf(a)) / sqrtf(b);
+    return r * r;
 }
 
 // The rotation of a pair in the form
@@ -78,18 +86,19 @@ struct Rot {
     cf sigma;
 };
 
-// Rotation parameters for g2 = |gamma|^2 > 0 from quantities scaled by
-// 1/(a+b) (no overflow or underflow for any representable norms):
+// Rotation parameters for gamma != 0 from quantities scaled by u = 1/(a+b)
+// (gamma u is squared, not gamma: no overflow or underflow for a + b >= 1e-36):
 // t = sign(b-a) 2|gamma| / (|b-a| + sqrt((b-a)^2 + 4|gamma|^2)),
 // c = 1/sqrt(1+t^2) (approximate reciprocal square root refined by one
 // Newton step), s = c t.  |sigma|^2 and tp come from the same c^2 t^2, so
 // rounding perturbs a rotated column's norm by a few ulps times s^2 only.
-__device__ __forceinline__ Rot make_rot(float a, float b, cf gam, float g2) {
+__device__ __forceinline__ Rot make_rot(float a, float b, cf gam) {
     const float ab = a + b;
     const float u = ab >= 1e-30f ? __fdividef(1.f, ab) : 1.f / ab;
     const float p = b - a;
     const float ph = p * u;                              // in [-1, 1]
-    const float gh = (g2 * u) * u;                       // in (0, 1/4]
+    const float gx = gam.x * u, gy = gam.y * u;
+    const float gh = fmaf(gx, gx, gy * gy);              // |gamma|^2 u^2, in (0, 1/4]
     const float h = fmaf(ph, ph, 4.f * gh);
     const float th = __fdividef(2.f, fabsf(ph) + h * rsqrtf(h));   // |t| / (|gamma| u)
     const float t2 = gh * th * th;                       // t^2 <= 1
@@ -101,7 +110,7 @@ __device__ __forceinline__ Rot make_rot(float a, float b, cf gam, float g2) {
     Rot r;
     r.sigma = cmake(k * gam.x, -k * gam.y);
     r.tp = __fdividef(c * c * t2, 1.f + c);
-    r.dn = sg * g2 * u * th;
+    r.dn = sg * gh * th * ab;                            // = sg |gamma|^2 u th
     return r;
 }
 
@@ -247,10 +256,10 @@ __device__ __forceinline__ bool visit_full(const mps_2q_job* __restrict__ jobs, 
         gam.x = warp_sum(gam.x);
         gam.y = warp_sum(gam.y);
         const float g2 = cabs2(gam);
-        const float r2 = pair_cos2(g2, a, b);
+        const float r2 = pair_cos2(gam, g2, a, b);
         offmax = fmaxf(offmax, r2);
         if (r2 > tol2) {                        // warp-uniform (butterfly sums)
-            const Rot R = make_rot(a, b, gam, g2);
+            const Rot R = make_rot(a, b, gam);
             float na = 0.f, nq = 0.f;
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) {
@@ -355,10 +364,10 @@ __device__ __forceinline__ void visit_ring(const mps_2q_job* __restrict__ jobs, 
         gam.x = warp_sum(gam.x);
         gam.y = warp_sum(gam.y);
         const float g2 = cabs2(gam);
-        const float r2 = pair_cos2(g2, hn, vn);
+        const float r2 = pair_cos2(gam, g2, hn, vn);
         offmax = fmaxf(offmax, r2);
         if (r2 > tol2) {
-            const Rot R = make_rot(hn, vn, gam, g2);
+            const Rot R = make_rot(hn, vn, gam);
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) apply_rot(R, hx[i], vx[i]);
             // closed-form norm update (Hestenes): |x'|^2 = |x|^2 - t|gamma|,
@@ -534,10 +543,10 @@ __device__ __forceinline__ bool visit_ring_handoff(const mps_2q_job* __restrict_
         gam.x = warp_sum(gam.x);
         gam.y = warp_sum(gam.y);
         const float g2 = cabs2(gam);
-        const float r2 = pair_cos2(g2, hn, vn);
+        const float r2 = pair_cos2(gam, g2, hn, vn);
         offmax = fmaxf(offmax, r2);
         if (r2 > tol2) {                        // warp-uniform (butterfly sums)
-            const Rot R = make_rot(hn, vn, gam, g2);
+            const Rot R = make_rot(hn, vn, gam);
 #pragma unroll
             for (int i = 0; i < ROWS; ++i) apply_rot(R, hx[i], vx[i]);
 #pragma unroll
@@ -1548,6 +1557,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (rc) return rc;
     rc = scale_theta(jobs, njobs, g, s);
     if (rc) return rc;
+    rc = lq_precondition(jobs, njobs, max_m, max_n, g, s);
+    if (rc) return rc;
 
     const int cmax = min(max_m, max_n);
     int nbmax = (cmax + bc - 1) / bc;
@@ -1766,6 +1777,8 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     rc = merge_gate_launch(jobs, njobs, max_chil, max_chir, g, s);
     if (rc) return rc;
     rc = scale_theta(jobs, njobs, g, s);
+    if (rc) return rc;
+    rc = lq_precondition(jobs, njobs, max_m, max_n, g, s);
     if (rc) return rc;
 
     const int cmax = min(max_m, max_n);

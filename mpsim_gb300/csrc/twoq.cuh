@@ -61,6 +61,11 @@ __host__ __device__ __forceinline__ bool job_tracks_v(int m, int n, int keep_lef
 // exact zeros: the isometric factor gets an orthonormal completion there.
 constexpr float kZeroSigma = 1e-30f;
 
+// Replaces X by its L factor (X = L Q) for the jobs whose left factor comes
+// from the final columns (lq.cu); the sweeps then need fewer passes.
+int lq_precondition(const mps_2q_job* jobs, int njobs, int max_m, int max_n, const TwoQGeom& g,
+                    cudaStream_t s);
+
 int merge_gate_launch(const mps_2q_job* jobs, int njobs, int max_chil, int max_chir,
                       const TwoQGeom& g, cudaStream_t s);
 

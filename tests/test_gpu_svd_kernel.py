@@ -158,6 +158,58 @@ def test_full_size_job(built_lib, cuda, chi, d, k):
         assert p.sweeps_out < 40
 
 
+def test_lq_preconditioned_mixed_batch(built_lib, cuda):
+    """Tall and square left-canonical jobs of 64 to 768 columns are solved on
+    the L factor of theta (theta = L Q, blocked Householder from the right);
+    a batch mixing them with wide, right-canonical and narrow jobs, a ragged
+    last panel (90 columns) and tall jobs (rows below the last panel) must
+    match LAPACK like every other job."""
+    rng = np.random.default_rng(23)
+    shapes = [  # chil, chim, chir, k, lc  (d = 2)
+        (128, 96, 128, 200, True),      # 256 x 256
+        (100, 60, 45, 70, True),        # tall 200 x 90: last panel 26 rows
+        (192, 64, 64, 100, True),       # tall 384 x 128
+        (96, 64, 96, 150, False),       # right-canonical: not factorised
+        (16, 32, 64, 20, True),         # wide 32 x 128: not factorised
+        (16, 8, 16, 32, True),          # 32 x 32: below the size threshold
+    ]
+    specs = []
+    for chil, chim, chir, k, lc in shapes:
+        a, b, g = make_job_inputs(rng, chil, chim, chir, 2, scale=1.0 / chim)
+        specs.append((a, b, g, k, lc))
+    rc, res, p = run_batch(built_lib, cuda, specs)
+    assert rc == 0, _native.last_error()
+    for spec, out in zip(specs, res):
+        check_job(spec, out, 2)
+
+
+@pytest.mark.parametrize("lc", [True, False])
+def test_graded_spectrum_keeps_isometry(built_lib, cuda, lc):
+    """Singular values spread over twelve decades, all kept.  Pairs of
+    columns below ~1e-10 in norm have |gamma|^2 below FP32's normal range
+    (the L factor's columns are graded like this from the first sweep); the
+    rotation test and angles must still see them, or the kept factor loses
+    its isometry in those directions."""
+    rng = np.random.default_rng(31)
+    a, b, g = make_job_inputs(rng, 128, 128, 128, 2, scale=1.0 / 128)
+    a = (a * (10.0 ** (-12.0 * np.arange(128) / 127))).astype(np.complex64)
+    rc, res, _ = run_batch(built_lib, cuda, [(a, b, g, 256, lc)])
+    assert rc == 0, _native.last_error()
+    check_job((a, b, g, 256, lc), res[0], 2)
+
+
+@pytest.mark.parametrize("chi", [384, 400])
+def test_lq_size_limit(built_lib, cuda, chi):
+    """768 columns is the widest factorised job (its 32-row panel fills the
+    shared memory); 800 columns is solved on theta itself."""
+    rng = np.random.default_rng(chi)
+    a, b, g = make_job_inputs(rng, chi, chi // 2, chi, 2, scale=1.0 / chi)
+    rc, res, p = run_batch(built_lib, cuda, [(a, b, g, chi, True)])
+    assert rc == 0, _native.last_error()
+    check_job((a, b, g, chi, True), res[0], 2)
+    assert p.sweeps_out < 40
+
+
 @pytest.mark.parametrize("scale", [1e-20, 1e-9, 1e15])
 def test_scale_invariance(built_lib, cuda, scale):
     """theta scaled far from 1: squared norms of 1e-40 are below FP32's
