@@ -70,53 +70,78 @@ lq_panel_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     cf* zz = P + (size_t)LQ_B * ps;             // [LQ_B][LQ_B]: (V^H V)[a][b], a < b
     cf* Ts = zz + LQ_B * LQ_B;                  // [LQ_B][LQ_B]: T, row-major
     cf* tau = Ts + LQ_B * LQ_B;                 // [LQ_B]
+    cf* invs = tau + LQ_B;                      // [LQ_B]: 1 / (y0 - beta)
+    float* betas = reinterpret_cast<float*>(invs + LQ_B);   // [LQ_B]
+    float* tail = betas + LQ_B;                 // [2]: |row i|^2 beyond its diagonal
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     cf* X = g.X + (size_t)j * g.lslot * g.cslot;
 
+#pragma unroll 4
     for (int e = tid; e < kb * nc; e += LQ_T) {
         const int r = e % kb, c = e / kb;
         P[r * ps + c] = X[(size_t)(k0 + c) * g.lslot + k0 + r];
     }
     __syncthreads();
+    if (warp == 0) {
+        float s = 0.f;
+        for (int c = 1 + lane; c < nc; c += 32) s += cabs2(P[c]);
+        s = warp_sum(s);
+        if (lane == 0) tail[0] = s;
+    }
+    __syncthreads();
 
+    // One barrier per reflector.  Every thread derives H_i from row i's
+    // diagonal entry and tail norm (left by the warp that updated row i in the
+    // step before); the rows below use row i unscaled (v = conj(x) inv), and
+    // row i becomes (beta, v) only after the loop.
     for (int i = 0; i < kb; ++i) {
-        cf* row = P + (size_t)i * ps;
-        if (warp == 0) {
-            float s = 0.f;
-            for (int c = i + 1 + lane; c < nc; c += 32) s += cabs2(row[c]);
-            s = warp_sum(s);
-            const cf y0 = cconj(row[i]);
-            cf t = cmake(0.f, 0.f), inv = cmake(0.f, 0.f);
-            float beta = y0.x;
-            if (s > 0.f || y0.y != 0.f) {
-                const float nrm = sqrtf(cabs2(y0) + s);
-                beta = y0.x >= 0.f ? -nrm : nrm;
-                t = cmake((beta - y0.x) / beta, -y0.y / beta);
-                inv = cinv(cmake(y0.x - beta, y0.y));
-            }
-            // v_i[c] = conj(x_i[c]) / (y0 - beta), stored where row i is now zero
-            for (int c = i + 1 + lane; c < nc; c += 32) row[c] = cmul(cconj(row[c]), inv);
-            __syncwarp();
-            if (lane == 0) {
-                tau[i] = t;
-                row[i] = cmake(beta, 0.f);
-            }
+        const cf* x = P + (size_t)i * ps;
+        const cf y0 = cconj(x[i]);
+        const float s = tail[i & 1];
+        cf t = cmake(0.f, 0.f), inv = cmake(0.f, 0.f);
+        float beta = y0.x;
+        if (s > 0.f || y0.y != 0.f) {
+            const float nrm = sqrtf(cabs2(y0) + s);
+            beta = y0.x >= 0.f ? -nrm : nrm;
+            t = cmake((beta - y0.x) / beta, -y0.y / beta);
+            inv = cinv(cmake(y0.x - beta, y0.y));
         }
-        __syncthreads();
-        // rows below: z <- z H_i = z - tau (z v) v^H  (v[i] = 1)
-        const cf t = tau[i];
+        if (tid == 0) {
+            tau[i] = t;
+            invs[i] = inv;
+            betas[i] = beta;
+        }
+        // z <- z H_i: d = z v = z[i] + inv sum_c z[c] conj(x[c]);
+        // z[i] -= tau d, z[c] -= tau d conj(inv) x[c]
         for (int r = i + 1 + warp; r < kb; r += LQ_NW) {
             cf* z = P + (size_t)r * ps;
-            cf d = lane == 0 ? z[i] : cmake(0.f, 0.f);
-            for (int c = i + 1 + lane; c < nc; c += 32) cfma(d, z[c], row[c]);
-            d.x = warp_sum(d.x);
-            d.y = warp_sum(d.y);
-            const cf td = cmul(t, d);
-            if (lane == 0) z[i] = csub(z[i], td);
-            for (int c = i + 1 + lane; c < nc; c += 32) z[c] = csub(z[c], cmul(td, cconj(row[c])));
+            const cf zi = z[i];
+            cf acc = cmake(0.f, 0.f);
+            for (int c = i + 1 + lane; c < nc; c += 32) cfma_conj(acc, x[c], z[c]);
+            acc.x = warp_sum(acc.x);
+            acc.y = warp_sum(acc.y);
+            const cf td = cmul(t, cadd(zi, cmul(inv, acc)));
+            const cf kx = cmul(td, cconj(inv));
+            if (lane == 0) z[i] = csub(zi, td);
+            float nn = 0.f;
+            for (int c = i + 1 + lane; c < nc; c += 32) {
+                const cf zc = csub(z[c], cmul(kx, x[c]));
+                z[c] = zc;
+                if (c > i + 1) nn += cabs2(zc);
+            }
+            if (r == i + 1) {
+                nn = warp_sum(nn);
+                if (lane == 0) tail[(i + 1) & 1] = nn;
+            }
         }
         __syncthreads();
     }
+    for (int e = tid; e < kb * nc; e += LQ_T) {
+        const int i = e / nc, c = e - (e / nc) * nc;
+        if (c > i) P[(size_t)i * ps + c] = cmul(cconj(P[(size_t)i * ps + c]), invs[i]);
+        else if (c == i) P[(size_t)i * ps + c] = cmake(betas[i], 0.f);
+    }
+    __syncthreads();
 
     // (V^H V)[a][b] for a < b, with V[c][a] = 0 (c < a), 1 (c = a), P[a][c] (c > a)
     for (int pi = warp; pi < kb * kb; pi += LQ_NW) {
@@ -179,7 +204,9 @@ lq_panel_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     }
 }
 
-// Rows k0+kb .. L-1 of the job: R <- R - (R V) Y, 64 rows per CTA.
+// Rows k0+kb .. L-1 of the job: R <- R - (R V) Y, 64 rows per CTA, in
+// 32-column chunks; each chunk's global loads are issued while the previous
+// chunk is being multiplied.
 __global__ void __launch_bounds__(256)
 lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     __shared__ cf Xs[32][LQ_TR];
@@ -197,21 +224,38 @@ lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     cf* X = g.X + (size_t)j * g.lslot * g.cslot;
     const cf* Vg = g.V + (size_t)j * g.cslot * g.cslot;
     const cf* Yg = Vg + (size_t)LQ_B * g.cslot;
+    const cf zero = cmake(0.f, 0.f);
 
-    // W[r][b] = sum_c X[r][k0 + c] V[c][b]; this thread: b = q*8 .. q*8+7
+    // W[r][b] = sum_c X[r][k0 + c] V[c][b]; this thread: b = q*8 .. q*8+7.
+    // Staging: element q2*256 + tid of a chunk is X column (q2*256+tid)/64,
+    // row (tid % 64), and V row (q2*256+tid)/32, column tid % 32.
+    cf xr[8], vr[4];
+    auto fetch1 = [&](int c0) {
+#pragma unroll
+        for (int q2 = 0; q2 < 8; ++q2) {
+            const int cc = (q2 * 256 + tid) / LQ_TR, c = c0 + cc, rg = row0 + rr;
+            xr[q2] = (c < nc && rg < L) ? X[(size_t)(k0 + c) * g.lslot + rg] : zero;
+        }
+#pragma unroll
+        for (int q2 = 0; q2 < 4; ++q2) {
+            const int e = q2 * 256 + tid, c = c0 + e / LQ_B;
+            vr[q2] = c < nc ? Vg[(size_t)c * LQ_B + (e % LQ_B)] : zero;
+        }
+    };
     cf acc[8];
 #pragma unroll
-    for (int b = 0; b < 8; ++b) acc[b] = cmake(0.f, 0.f);
+    for (int b = 0; b < 8; ++b) acc[b] = zero;
+    fetch1(0);
     for (int c0 = 0; c0 < nc; c0 += 32) {
-        for (int e = tid; e < 32 * LQ_TR; e += 256) {
-            const int cc = e / LQ_TR, rl = e % LQ_TR, c = c0 + cc, rg = row0 + rl;
-            Xs[cc][rl] = (c < nc && rg < L) ? X[(size_t)(k0 + c) * g.lslot + rg] : cmake(0.f, 0.f);
-        }
-        for (int e = tid; e < 32 * LQ_B; e += 256) {
-            const int cc = e / LQ_B, b = e % LQ_B, c = c0 + cc;
-            Bs[cc][b] = c < nc ? Vg[(size_t)c * LQ_B + b] : cmake(0.f, 0.f);
+#pragma unroll
+        for (int q2 = 0; q2 < 8; ++q2) Xs[(q2 * 256 + tid) / LQ_TR][rr] = xr[q2];
+#pragma unroll
+        for (int q2 = 0; q2 < 4; ++q2) {
+            const int e = q2 * 256 + tid;
+            Bs[e / LQ_B][e % LQ_B] = vr[q2];
         }
         __syncthreads();
+        if (c0 + 32 < nc) fetch1(c0 + 32);
 #pragma unroll 4
         for (int cc = 0; cc < 32; ++cc) {
             const cf x = Xs[cc][rr];
@@ -222,27 +266,41 @@ lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     }
 #pragma unroll
     for (int b = 0; b < 8; ++b) Ws[q * 8 + b][rr] = acc[b];
-    __syncthreads();
 
-    // X[r][k0 + c] -= sum_b W[r][b] Y[b][c]; this thread: columns q*8 .. q*8+7 of each chunk
-    for (int c0 = 0; c0 < nc; c0 += 32) {
-        for (int e = tid; e < LQ_B * 32; e += 256) {
-            const int b = e / 32, cc = e % 32, c = c0 + cc;
-            Bs[b][cc] = c < nc ? Yg[(size_t)b * g.cslot + c] : cmake(0.f, 0.f);
+    // X[r][k0 + c] -= sum_b W[r][b] Y[b][c]; this thread: columns q*8 .. q*8+7
+    // of each chunk (its row's entries are fetched a chunk ahead, with Y)
+    cf yr[4], zr[8];
+    auto fetch2 = [&](int c0) {
+#pragma unroll
+        for (int q2 = 0; q2 < 4; ++q2) {
+            const int e = q2 * 256 + tid, c = c0 + (e % 32);
+            yr[q2] = c < nc ? Yg[(size_t)(e / 32) * g.cslot + c] : zero;
         }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int c = c0 + q * 8 + k;
+            zr[k] = (live && c < nc) ? X[(size_t)(k0 + c) * g.lslot + r] : zero;
+        }
+    };
+    fetch2(0);
+    for (int c0 = 0; c0 < nc; c0 += 32) {
+#pragma unroll
+        for (int q2 = 0; q2 < 4; ++q2) {
+            const int e = q2 * 256 + tid;
+            Bs[e / 32][e % 32] = yr[q2];
+        }
+        cf z[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) z[k] = zr[k];
         __syncthreads();
-        if (live) {
-#pragma unroll 2
-            for (int k = 0; k < 8; ++k) {
-                const int cc = q * 8 + k, c = c0 + cc;
-                if (c < nc) {
-                    cf s = cmake(0.f, 0.f);
+        if (c0 + 32 < nc) fetch2(c0 + 32);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int cc = q * 8 + k, c = c0 + cc;
+            cf s = cmake(0.f, 0.f);
 #pragma unroll 8
-                    for (int b = 0; b < LQ_B; ++b) cfma(s, Ws[b][rr], Bs[b][cc]);
-                    cf* px = X + (size_t)(k0 + c) * g.lslot + r;
-                    *px = csub(*px, s);
-                }
-            }
+            for (int b = 0; b < LQ_B; ++b) cfma(s, Ws[b][rr], Bs[b][cc]);
+            if (live && c < nc) X[(size_t)(k0 + c) * g.lslot + r] = csub(z[k], s);
         }
         __syncthreads();
     }
@@ -272,13 +330,13 @@ int lq_precondition(const mps_2q_job* jobs, int njobs, int max_m, int max_n, con
     if (cmax < LQ_MIN_C) return MPS_OK;
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
-    const size_t smem_max = ((size_t)LQ_B * (LQ_MAX_C + 1) + 2 * LQ_B * LQ_B + LQ_B) * sizeof(cf);
+    const size_t smem_max = ((size_t)LQ_B * (LQ_MAX_C + 1) + 2 * LQ_B * LQ_B + 3 * LQ_B) * sizeof(cf);
     std::call_once(once, [&] {
         attr = cudaFuncSetAttribute(lq_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem_max);
     });
     if (attr != cudaSuccess) return cuda_fail(attr, "cudaFuncSetAttribute(lq_panel_kernel)");
-    const size_t smem = ((size_t)LQ_B * (cmax + 1) + 2 * LQ_B * LQ_B + LQ_B) * sizeof(cf);
+    const size_t smem = ((size_t)LQ_B * (cmax + 1) + 2 * LQ_B * LQ_B + 3 * LQ_B) * sizeof(cf);
     for (int k0 = 0; k0 < cmax; k0 += LQ_B) {
         lq_panel_kernel<<<njobs, LQ_T, smem, s>>>(jobs, g, k0);
         MPS_LAUNCH_CHECK("lq_panel_kernel");
