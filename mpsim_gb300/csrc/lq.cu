@@ -25,11 +25,11 @@
 //     tau = (beta - y0) / beta, v = (1, y_1.. / (y0 - beta))), applied at once
 //     to the panel rows below; then the compact WY factor
 //     H_0 ... H_{kb-1} = I - V T V^H (T upper triangular,
-//     T[0:i, i] = -tau_i T[0:i, 0:i] V[:, 0:i]^H v_i) and Y = T V^H.
+//     T[0:i, i] = -tau_i T[0:i, 0:i] V[:, 0:i]^H v_i).
 //   lq_trail_kernel (job x 64-row tiles): the rows below the panel,
-//     R <- R (I - V T V^H) = R - (R V) Y.
-// V (nc x LQ_B) and Y (LQ_B x nc) of the current panel live in the job's V
-// slot, which jobs of this kind do not otherwise use before the Gram step
+//     R <- R (I - V T V^H) = R - ((R V) T) V^H.
+// V (nc x LQ_B) and T (LQ_B x LQ_B) of the current panel live in the job's
+// V slot, which jobs of this kind do not otherwise use before the Gram step
 // after the sweeps.
 #include <mutex>
 
@@ -174,26 +174,18 @@ lq_panel_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     }
     __syncthreads();
 
-    // V (nc x LQ_B, zero beyond kb) and Y = T V^H (LQ_B x nc) to the V slot
+    // V (nc x LQ_B, zero beyond kb) and T (LQ_B x LQ_B) to the V slot
     cf* Vg = g.V + (size_t)j * g.cslot * g.cslot;
-    cf* Yg = Vg + (size_t)LQ_B * g.cslot;
+    cf* Tg = Vg + (size_t)LQ_B * g.cslot;
     for (int e = tid; e < nc * LQ_B; e += LQ_T) {
         const int c = e / LQ_B, b = e % LQ_B;
         cf v = cmake(0.f, 0.f);
         if (b < kb) v = c < b ? cmake(0.f, 0.f) : (c == b ? cmake(1.f, 0.f) : P[(size_t)b * ps + c]);
         Vg[e] = v;
     }
-    for (int e = tid; e < LQ_B * nc; e += LQ_T) {
-        const int a = e / nc, c = e - (e / nc) * nc;
-        cf y = cmake(0.f, 0.f);
-        if (a < kb) {
-            const int bmax = min(c, kb - 1);
-            for (int b = a; b <= bmax; ++b) {
-                const cf vcb = c == b ? cmake(1.f, 0.f) : P[(size_t)b * ps + c];
-                cfma(y, Ts[a * LQ_B + b], cconj(vcb));
-            }
-        }
-        Yg[(size_t)a * g.cslot + c] = y;
+    for (int e = tid; e < LQ_B * LQ_B; e += LQ_T) {
+        const int a = e / LQ_B, b = e % LQ_B;
+        Tg[e] = (a < kb && b < kb && b >= a) ? Ts[e] : cmake(0.f, 0.f);
     }
     // the panel's rows of L: left of the diagonal as transformed, beta on it,
     // zero right of it
@@ -204,14 +196,18 @@ lq_panel_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     }
 }
 
-// Rows k0+kb .. L-1 of the job: R <- R - (R V) Y, 64 rows per CTA, in
-// 32-column chunks; each chunk's global loads are issued while the previous
-// chunk is being multiplied.
+// Rows k0+kb .. L-1 of the job: R <- R - ((R V) T) V^H, 64 rows per CTA,
+// in 32-column chunks; each chunk's global loads are issued while the
+// previous chunk is being multiplied.
 __global__ void __launch_bounds__(256)
 lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
-    __shared__ cf Xs[32][LQ_TR];
-    __shared__ cf Bs[32][LQ_B];
-    __shared__ cf Ws[LQ_B][LQ_TR];
+    // phase 1: Xs [32][LQ_TR] and Bs [32][LQ_B] (a V chunk, then T);
+    // phase 2: Vt [LQ_B][33] (a conjugated V chunk, transposed) over Xs
+    __shared__ cf sm[32 * LQ_TR + 32 * LQ_B + LQ_B * LQ_TR];
+    cf (*Xs)[LQ_TR] = reinterpret_cast<cf (*)[LQ_TR]>(sm);
+    cf (*Vt)[33] = reinterpret_cast<cf (*)[33]>(sm);
+    cf (*Bs)[LQ_B] = reinterpret_cast<cf (*)[LQ_B]>(sm + 32 * LQ_TR);
+    cf (*Ws)[LQ_TR] = reinterpret_cast<cf (*)[LQ_TR]>(sm + 32 * LQ_TR + 32 * LQ_B);
     const int j = blockIdx.y;
     int L, C;
     if (!lq_job(jobs[j], g.d, L, C) || k0 >= C) return;
@@ -223,18 +219,18 @@ lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     const bool live = r < L;
     cf* X = g.X + (size_t)j * g.lslot * g.cslot;
     const cf* Vg = g.V + (size_t)j * g.cslot * g.cslot;
-    const cf* Yg = Vg + (size_t)LQ_B * g.cslot;
+    const cf* Tg = Vg + (size_t)LQ_B * g.cslot;
     const cf zero = cmake(0.f, 0.f);
 
     // W[r][b] = sum_c X[r][k0 + c] V[c][b]; this thread: b = q*8 .. q*8+7.
-    // Staging: element q2*256 + tid of a chunk is X column (q2*256+tid)/64,
-    // row (tid % 64), and V row (q2*256+tid)/32, column tid % 32.
+    // Staging: element q2*256 + tid of a chunk is X column q2*4 + q, row rr,
+    // and V row (q2*256+tid)/32, column tid % 32.
     cf xr[8], vr[4];
     auto fetch1 = [&](int c0) {
 #pragma unroll
         for (int q2 = 0; q2 < 8; ++q2) {
-            const int cc = (q2 * 256 + tid) / LQ_TR, c = c0 + cc, rg = row0 + rr;
-            xr[q2] = (c < nc && rg < L) ? X[(size_t)(k0 + c) * g.lslot + rg] : zero;
+            const int c = c0 + q2 * 4 + q;
+            xr[q2] = (c < nc && live) ? X[(size_t)(k0 + c) * g.lslot + r] : zero;
         }
 #pragma unroll
         for (int q2 = 0; q2 < 4; ++q2) {
@@ -248,7 +244,7 @@ lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
     fetch1(0);
     for (int c0 = 0; c0 < nc; c0 += 32) {
 #pragma unroll
-        for (int q2 = 0; q2 < 8; ++q2) Xs[(q2 * 256 + tid) / LQ_TR][rr] = xr[q2];
+        for (int q2 = 0; q2 < 8; ++q2) Xs[q2 * 4 + q][rr] = xr[q2];
 #pragma unroll
         for (int q2 = 0; q2 < 4; ++q2) {
             const int e = q2 * 256 + tid;
@@ -264,17 +260,34 @@ lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
         }
         __syncthreads();
     }
+    // W <- W T (T upper triangular)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) Ws[q * 8 + b][rr] = acc[b];
+#pragma unroll
+    for (int q2 = 0; q2 < 4; ++q2) {
+        const int e = q2 * 256 + tid;
+        Bs[e / LQ_B][e % LQ_B] = Tg[e];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const int bb = q * 8 + b;
+        cf w = zero;
+        for (int a = 0; a <= bb; ++a) cfma(w, Ws[a][rr], Bs[a][bb]);
+        acc[b] = w;
+    }
+    __syncthreads();
 #pragma unroll
     for (int b = 0; b < 8; ++b) Ws[q * 8 + b][rr] = acc[b];
 
-    // X[r][k0 + c] -= sum_b W[r][b] Y[b][c]; this thread: columns q*8 .. q*8+7
-    // of each chunk (its row's entries are fetched a chunk ahead, with Y)
-    cf yr[4], zr[8];
+    // X[r][k0 + c] -= sum_b W[r][b] conj(V[c][b]); this thread: columns
+    // q*8 .. q*8+7 of each chunk (its row's entries fetched a chunk ahead)
+    cf zr[8];
     auto fetch2 = [&](int c0) {
 #pragma unroll
         for (int q2 = 0; q2 < 4; ++q2) {
-            const int e = q2 * 256 + tid, c = c0 + (e % 32);
-            yr[q2] = c < nc ? Yg[(size_t)(e / 32) * g.cslot + c] : zero;
+            const int e = q2 * 256 + tid, c = c0 + e / LQ_B;
+            vr[q2] = c < nc ? Vg[(size_t)c * LQ_B + (e % LQ_B)] : zero;
         }
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
@@ -287,7 +300,7 @@ lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
 #pragma unroll
         for (int q2 = 0; q2 < 4; ++q2) {
             const int e = q2 * 256 + tid;
-            Bs[e / 32][e % 32] = yr[q2];
+            Vt[e % LQ_B][e / LQ_B] = cconj(vr[q2]);
         }
         cf z[8];
 #pragma unroll
@@ -299,7 +312,7 @@ lq_trail_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int k0) {
             const int cc = q * 8 + k, c = c0 + cc;
             cf s = cmake(0.f, 0.f);
 #pragma unroll 8
-            for (int b = 0; b < LQ_B; ++b) cfma(s, Ws[b][rr], Bs[b][cc]);
+            for (int b = 0; b < LQ_B; ++b) cfma(s, Ws[b][rr], Vt[b][cc]);
             if (live && c < nc) X[(size_t)(k0 + c) * g.lslot + r] = csub(z[k], s);
         }
         __syncthreads();
