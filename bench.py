@@ -48,9 +48,9 @@ def gate_flops(m, n, chim, d):
 
 
 # DRAM bytes (read + write) of one mps_apply_2q_batch call on a chi=256 layer of
-# the default workload, summed over its 69 launches from one ncu capture
+# the default workload, summed over its 79 launches from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum; profiles/traffic_2q_call_chi256.md).
-CALL_TRAFFIC_BYTES = 3.0625e9
+CALL_TRAFFIC_BYTES = 1.856e9
 
 
 def replica_instance(rank: int) -> int:

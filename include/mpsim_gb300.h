@@ -112,7 +112,11 @@ size_t mps_2q_workspace_bytes(int njobs, int max_m, int max_n, int d);
  * A.B with the gate fused in (theta = (chi_l*d) x (d*chi_r)), block one-sided
  * Jacobi SVD, descending sort, truncation to k values, and the regauge with
  * the singular values placed as keep_left_canonical asks.  max_m/max_n bound
- * every job's theta; the host must know them.  Blocks the calling thread
+ * every job's theta; the host must know them.  Left-canonical jobs with
+ * m >= n and 64 <= n <= 768 run the Jacobi sweeps on the L factor of theta
+ * (theta = L Q, Householder from the right), which needs fewer sweeps and
+ * leaves the singular values and left vectors unchanged; the right factor
+ * is then formed as U^H theta.  Blocks the calling thread
  * once per Jacobi sweep to test convergence, and returns after the last
  * sweep with the sort, regauge and output kernels still queued on the stream
  * (the outputs are stream-ordered like any kernel's).
