@@ -44,6 +44,9 @@ constexpr int LQ_NW = LQ_T / 32;
 constexpr int LQ_TR = 64;       // rows per trailing-update CTA
 constexpr int LQ_MIN_C = 64;    // narrower jobs converge in a few cheap sweeps anyway
 constexpr int LQ_MAX_C = 768;   // the panel (LQ_B x (C+1)) must fit in shared memory
+// V (C x LQ_B) and T (LQ_B x LQ_B, at offset LQ_B * cslot) must fit in the
+// job's cslot x cslot V slot; cslot >= C >= LQ_MIN_C
+static_assert(LQ_MIN_C * LQ_MIN_C >= LQ_B * (LQ_MIN_C + LQ_B), "V slot too small for V and T");
 
 // Jobs that are factorised, and their shape (X is L x C).
 __device__ __forceinline__ bool lq_job(const mps_2q_job& job, int d, int& L, int& C) {
