@@ -39,7 +39,7 @@ namespace mps {
 namespace {
 
 constexpr int LQ_B = 32;        // rows per panel
-constexpr int LQ_T = 512;       // threads of the panel kernel
+constexpr int LQ_T = 1024;      // threads of the panel kernel: a warp per panel row
 constexpr int LQ_NW = LQ_T / 32;
 constexpr int LQ_TR = 64;       // rows per trailing-update CTA
 constexpr int LQ_MIN_C = 64;    // narrower jobs converge in a few cheap sweeps anyway
