@@ -145,15 +145,11 @@ def _time_call(fn, min_seconds=0.02):
 
 
 def cpu_sample(circ, seed=123, budget=12.0):
-    """The reference's CPU algorithm (NumPy oracle port: merge, LAPACK SVD,
-    regauge; one-qudit contraction) timed on one gate of every distinct shape
-    of ``circ``, weighted by how often each shape occurs.  A short first pass
-    estimates each shape's cost; the ``budget`` seconds are then split over the
-    shapes by their share of the whole circuit's CPU time and each shape is
-    timed again for its share.  Returns (two-qudit gates/s over the whole
-    circuit, seconds spent timing, per-gate seconds of the per-gate norm sweep
-    the reference also runs, at the largest bond, number of two-qudit shapes,
-    number of one-qudit shapes)."""
+    """Cross-check of the reference arm: the NumPy oracle port (merge, LAPACK
+    SVD, regauge; one-qudit contraction) timed on one gate of every distinct
+    shape of ``circ``, weighted by how often each shape occurs, without the
+    reference's per-gate norm sweep.  Returns two-qudit gates/s over the whole
+    circuit and the seconds spent."""
     from oracle.ref_mps import OracleMPS
     from mpsim_gb300.circuits import haar_random_matrix
     rng = np.random.default_rng(seed)
@@ -190,47 +186,201 @@ def cpu_sample(circ, seed=123, budget=12.0):
     total = 0.0
     for (count, fn), e in zip(calls, est):
         total += count * _time_call(fn, max(0.005, left * e / sum(est)))
-    chi = max(c[1] for c in two)
-    a = rnd((chi, d, chi))
+    return sum(two.values()) / total, time.perf_counter() - t_start
 
-    def norm_step():
-        env = np.eye(chi, dtype=np.complex64)
-        t = np.tensordot(env, np.conj(a), axes=([1], [0]))
-        np.tensordot(a, t, axes=([0, 1], [0, 1]))
-    norm_per_gate = circ.nqudits * _time_call(norm_step)
-    ngates = sum(two.values())
-    return ngates / total, time.perf_counter() - t_start, norm_per_gate, len(two), len(one)
+
+REF_DIR = os.path.join(HERE, "baseline", "_ref")
+SHIM_DIR = os.path.join(HERE, "oracle", "tn_shim")
+
+
+def import_reference():
+    """The reference's own package (pip-installed, unmodified, into
+    baseline/_ref) over oracle/tn_shim -- a restatement of the TensorNetwork
+    0.2.1 subset it calls, which is not installed anywhere -- with the two
+    NumPy-2 patches it needs to import (``np.complex``, the ``newshape=``
+    keyword of ``np.reshape``).  Returns ((tensornetwork, mpsim.core), None)
+    or (None, reason)."""
+    if not os.path.isfile(os.path.join(REF_DIR, "mpsim", "core.py")):
+        return None, "baseline/_ref/mpsim is not installed"
+    for p in (SHIM_DIR, REF_DIR):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    if not hasattr(np, "complex"):
+        np.complex = complex
+    if not getattr(np.reshape, "_newshape_patch", False):
+        orig = np.reshape
+
+        def reshape(a, *args, **kw):
+            if "newshape" in kw:
+                kw["shape"] = kw.pop("newshape")
+            return orig(a, *args, **kw)
+        reshape._newshape_patch = True
+        np.reshape = reshape
+    try:
+        import tensornetwork as tn
+        import mpsim.core as core
+    except Exception as exc:          # pragma: no cover - depends on the host
+        return None, f"reference import failed: {exc!r}"
+    if not os.path.realpath(core.__file__).startswith(os.path.realpath(REF_DIR)):
+        return None, f"mpsim.core resolved to {core.__file__}, not baseline/_ref"
+    return (tn, core), None
+
+
+class ReferenceCircuit:
+    """One seeded circuit driven through the reference's own public API:
+    ``MPS.apply_one_qudit_gate`` / ``apply_two_qudit_gate(..., maxsvals=)``
+    with complex64 gates (mpsim/core.py:753-845, 950-1161).  ``as_shipped``
+    keeps the norm sweep the reference runs after every two-qudit gate
+    (``self._norms.append(self.norm())``, core.py:1160-1161); otherwise
+    ``MPS.norm`` is replaced by a constant for the duration of the layer."""
+
+    def __init__(self, circ, tn, core):
+        self.circ, self.tn, self.core = circ, tn, core
+        self.mps = core.MPS(circ.nqudits, circ.d)
+        self.next_layer = 0
+        self.steady_from = None
+
+    def run_layer(self, li, as_shipped=True):
+        circ, tn, mps = self.circ, self.tn, self.mps
+        lay = circ.layers[li]
+        d = circ.d
+        cls = type(mps)
+        orig_norm = cls.norm
+        if not as_shipped:
+            cls.norm = lambda self: 0.0
+        try:
+            t0 = time.perf_counter()
+            for i in range(circ.nqudits):
+                mps.apply_one_qudit_gate(tn.Node(lay.one_q[i].astype(np.complex64)), i)
+            for p, i in enumerate(lay.pair_left):
+                g = lay.two_q[p].astype(np.complex64).reshape((d,) * 4)
+                mps.apply_two_qudit_gate(tn.Node(g), int(i), int(i) + 1, maxsvals=circ.maxsvals)
+            return time.perf_counter() - t0, len(lay.pair_left)
+        finally:
+            cls.norm = orig_norm
+
+    def warm_to_steady(self):
+        """Runs (as shipped) the layers up to and including the first one whose
+        bonds are all at their final maximum; returns (seconds, two-qudit gates)."""
+        t = g = 0
+        final = max(C_gate_bonds(self.circ))
+        while self.next_layer < len(self.circ.layers):
+            dt, ng = self.run_layer(self.next_layer)
+            t += dt
+            g += ng
+            self.next_layer += 1
+            if max(self.mps.bond_dimensions()) >= final:
+                break
+        self.steady_from = self.next_layer
+        return t, g
+
+    def steady_layer(self, as_shipped=True):
+        """The next steady-state layer (wrapping around to the first steady layer
+        once the circuit ends: the bond dimensions stay at their maximum)."""
+        if self.next_layer >= len(self.circ.layers):
+            self.next_layer = self.steady_from
+        dt, ng = self.run_layer(self.next_layer, as_shipped)
+        self.next_layer += 1
+        return dt, ng
+
+
+def C_gate_bonds(circ):
+    from mpsim_gb300.circuits import gate_shapes
+    _, two = gate_shapes(circ)
+    return [max(k[0], k[2]) for k in two]
+
+
+def reference_rate(circ, steady_layers=1):
+    """CPU baseline of the reference itself: the circuit's first layers through
+    the first steady-state layer (timed), then ``steady_layers`` steady-state
+    layers as shipped and one with the per-gate norm disabled.  The whole-circuit
+    rate is extrapolated from the measured early part plus the steady-state rate
+    for the remaining gates.  Returns a dict, or None with a reason."""
+    ref, why = import_reference()
+    if ref is None:
+        return None, why
+    tn, core = ref
+    rc = ReferenceCircuit(circ, tn, core)
+    t0 = time.perf_counter()
+    t_early, g_early = rc.warm_to_steady()
+    ts = gs = 0
+    for _ in range(steady_layers):
+        dt, ng = rc.steady_layer(True)
+        ts += dt
+        gs += ng
+    dn, gn = rc.steady_layer(False)
+    ngates = circ.n_two_qudit_gates
+    rate = gs / ts
+    whole = ngates / (t_early + (ngates - g_early) / rate)
+    return {"whole": whole, "steady": rate, "steady_no_norms": gn / dn,
+            "early_s": t_early, "early_gates": g_early, "spent": time.perf_counter() - t0}, None
+
+
+def _blas_threads():
+    try:
+        from threadpoolctl import threadpool_info
+        return sum(int(i.get("num_threads", 0)) for i in threadpool_info()
+                   if i.get("user_api") == "blas") or None
+    except Exception:
+        return None
 
 
 def run_reference(args, rank, world):
+    """``--impl reference``: the reference's own MPS (baseline/_ref, unmodified,
+    over oracle/tn_shim) on the host cores, rank 0 only.  Setup (untimed): the
+    circuit's layers up to the first steady-state layer.  Warm-up steps: one
+    steady-state layer each with the per-gate norm sweep disabled (the second
+    variant).  Timed steps: one steady-state layer each as shipped.  ``value``
+    = the whole circuit's two-qudit gates over the measured early layers plus
+    the remaining gates at the timed steady-state rate."""
     if rank != 0:
         return 0
     from mpsim_gb300 import circuits as C
-    circ = C.workload(args.workload if args.workload in C.WORKLOADS else WORKLOAD)
-    for _ in range(args.warmup):
-        cpu_sample(circ, budget=2.0)
-    rates = []
+    name = args.workload if args.workload in C.WORKLOADS else WORKLOAD
+    circ = C.workload(name)
+    ref, why = import_reference()
+    if ref is None:
+        print(json.dumps({"impl": "reference", "unavailable": why}), flush=True)
+        return 0
+    tn, core = ref
+    rc = ReferenceCircuit(circ, tn, core)
+    t_early, g_early = rc.warm_to_steady()
+    nn_t = nn_g = 0
+    for _ in range(max(args.warmup, 1)):
+        dt, ng = rc.steady_layer(as_shipped=False)
+        nn_t += dt
+        nn_g += ng
+    ts = gs = 0
     t_all = time.perf_counter()
     for _ in range(args.steps):
-        rate, spent, norm_cost, n2, n1 = cpu_sample(circ, budget=10.0)
-        rates.append(rate)
+        dt, ng = rc.steady_layer(as_shipped=True)
+        ts += dt
+        gs += ng
     total = time.perf_counter() - t_all
-    value = float(np.mean(rates))
+    steady = gs / ts
+    ngates = circ.n_two_qudit_gates
+    value = ngates / (t_early + (ngates - g_early) / steady)
+    port, port_s = cpu_sample(circ, budget=3.0)
     cores = os.cpu_count()
-    sample = (f"NumPy oracle port of mpsim/core.py (merge, np.linalg.svd, regauge; one-qudit "
-              f"contraction) timed on one gate of each of the {n2} two-qudit and {n1} one-qudit "
-              f"shapes of the {circ.nqudits}-qubit depth-{circ.depth} circuit and weighted by their "
-              f"counts, {spent:.1f}s of timing per step, {cores} host threads; excludes the per-gate norm sweep the reference runs "
-              f"after every two-qudit gate (~{norm_cost:.3f}s per gate at chi=256)")
+    sample = (f"the reference's own mpsim.core (baseline/_ref, unmodified; TensorNetwork 0.2.1 "
+              f"restated in oracle/tn_shim) on {circ.nqudits}-qubit depth-{circ.depth} "
+              f"maxsvals={circ.maxsvals}: layers 0-{rc.steady_from - 1} timed once "
+              f"({g_early} gates, {t_early:.1f}s), then {args.steps} steady-state layers as shipped "
+              f"({gs} gates, {ts:.1f}s, per-gate norm sweep included); whole-circuit rate "
+              f"extrapolated from both; {cores} host threads")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
-        "data": "synthetic (seeded Haar gates, random sites of each gate shape)",
-        "config": {"workload": circ_name(circ), "sample": "shape-weighted gate sample"},
+        "data": "synthetic (seeded Haar gates)",
+        "config": {"workload": circ_name(circ), "sample": "steady-state layer per step",
+                   "same_config": True},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "reference",
+                         "sample": sample, "blas_threads": _blas_threads()},
+        "variants": {"as_shipped_steady": steady,
+                     "norms_disabled_steady": nn_g / nn_t if nn_t else None,
+                     "oracle_port_cross_check": port},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -331,6 +481,7 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncircuits", type=int, default=0)
+    ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -373,7 +524,7 @@ def main():
 
     def step_resident(timing=None):
         flush.fill_(1)
-        mps = MPS(circ.nqudits, d)
+        mps = MPS(circ.nqudits, d, precision=args.precision)
         mps.timing = timing
         for one, left, two in dev_layers:
             mps.apply_layer_resident(one, left, two, maxsvals=maxs)
@@ -381,7 +532,7 @@ def main():
 
     def step_e2e():
         flush.fill_(1)
-        mps = MPS(circ.nqudits, d)
+        mps = MPS(circ.nqudits, d, precision=args.precision)
         for one, left, two in host_layers:
             mps.apply_layer(one, left, two, maxsvals=maxs)
         return mps.norm()
@@ -396,7 +547,7 @@ def main():
 
     def step_apply_ops():
         flush.fill_(1)
-        mps = MPS(circ.nqudits, d)
+        mps = MPS(circ.nqudits, d, precision=args.precision)
         for ops in host_ops:
             mps.apply(ops, maxsvals=maxs)
         return mps.norm()
@@ -477,12 +628,17 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rate, dt, norm_cost, n2, n1 = cpu_sample(circ)
-        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"NumPy oracle port on one gate of each of the {n2} two-qudit and {n1} "
-                         f"one-qudit shapes of this circuit, weighted by their counts ({dt:.1f}s "
-                         f"of timing); excludes the reference's per-gate norm sweep "
-                         f"(~{norm_cost:.3f}s per gate at chi=256)"}
+        r, why = reference_rate(circ)
+        if r is not None:
+            cpu = {"value": r["whole"], "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                   "sample": (f"the reference's own mpsim.core over oracle/tn_shim: layers up to the "
+                              f"first steady-state one ({r['early_gates']} gates, {r['early_s']:.1f}s), "
+                              f"one steady-state layer as shipped and one with the per-gate norm "
+                              f"disabled ({r['spent']:.1f}s in all); whole-circuit rate extrapolated"),
+                   "steady": r["steady"], "steady_no_norms": r["steady_no_norms"]}
+        else:
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                   "sample": f"unavailable: {why}"}
 
     if rank == 0:
         line = {
@@ -492,7 +648,9 @@ def main():
             "data": "synthetic (seeded Haar gates)",
             "config": {"workload": args.workload, "nqudits": circ.nqudits, "depth": circ.depth,
                        "maxsvals": maxs, "two_qudit_gates_per_step": ngates,
-                       "precision": "plain complex64, FP32 SIMT",
+                       "precision": ("plain complex64, FP32 SIMT" if args.precision == "plain" else
+                                     "mixed: tcgen05 split-bf16 block Jacobi for left-canonical "
+                                     "gates of 64+ columns, FP32 SIMT elsewhere"),
                        "parallelism": f"replicas x{world}",
                        "l2": "256 MiB buffer written at the start of every step"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,

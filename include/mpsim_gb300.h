@@ -77,7 +77,22 @@ typedef struct {
     int32_t stall_test;    /* test hook: nonzero makes one wait target a
                               round that never completes, so the wait must
                               expire (with a small wait_limit)             */
+    int32_t precision;     /* MPS_PRECISION_PLAIN (default) or
+                              MPS_PRECISION_MIXED                          */
 } mps_svd_params;
+
+/* mps_svd_params.precision.
+ * PLAIN: complex64 with FP32 SIMT arithmetic throughout.
+ * MIXED: the Jacobi sweeps run as 32-column block pairs whose Gram matrices
+ *   G = Y^H Y and rotations Y <- Y Q are tcgen05 tensor-core GEMMs on bf16
+ *   operands (every FP32 value split into three bf16 pieces, six piece
+ *   products accumulated in FP32 in TMEM: FP32-grade products); the rotation
+ *   parameters come from G in shared memory, the off-diagonal test is FP64.
+ *   Every job of the call must be tall (m >= n) and left-canonical with at
+ *   least 64 columns (MPS_ERR_ARG otherwise); mpsim_gb300's Python layer
+ *   routes other jobs to a PLAIN call. */
+#define MPS_PRECISION_PLAIN 0
+#define MPS_PRECISION_MIXED 1
 
 /* Library version and build description. */
 int mps_version(void);
@@ -191,6 +206,21 @@ int mps_cgemm(void* stream, int m, int n, int k, const mps_c64* a, long long sam
               long long sak, int conj_a, const mps_c64* b, long long sbk,
               long long sbn, int conj_b, mps_c64* c, long long scm, long long scn,
               int batch, long long bsa, long long bsb, long long bsc);
+
+/* mps_cgemm on the tcgen05 tensor cores: same arguments and result, computed
+ * as a real GEMM on the complex embedding with every FP32 operand split into
+ * three bf16 pieces and the six piece products of order <= 2 accumulated in
+ * FP32 in TMEM (as accurate as FP32 arithmetic).  The overlap, wavefunction
+ * and reduced-density-matrix sweeps (mpsim/core.py:483-565, 596-653) use it
+ * where their contractions are compute-bound. */
+int mps_cgemm_tc(void* stream, int m, int n, int k, const mps_c64* a, long long sam,
+                 long long sak, int conj_a, const mps_c64* b, long long sbk,
+                 long long sbn, int conj_b, mps_c64* c, long long scm, long long scn,
+                 int batch, long long bsa, long long bsb, long long bsc);
+
+/* Reads and clears the flag the tensor-core kernels set when one of their
+ * bounded mbarrier waits expired (their outputs are then invalid).  Blocks. */
+int mps_tc_error(int* flag_out);
 
 /* Workspace for mps_site_marginals: every left environment plus two
  * right environments and two (chi, d, chi) scratch tensors. */

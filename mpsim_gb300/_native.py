@@ -47,7 +47,12 @@ assert JOB1_DTYPE.itemsize == 24
 class SvdParams(ctypes.Structure):
     _fields_ = [("max_sweeps", ctypes.c_int32), ("tol", ctypes.c_float),
                 ("block_cols", ctypes.c_int32), ("sweeps_out", ctypes.c_int32),
-                ("wait_limit", ctypes.c_int32), ("stall_test", ctypes.c_int32)]
+                ("wait_limit", ctypes.c_int32), ("stall_test", ctypes.c_int32),
+                ("precision", ctypes.c_int32)]
+
+
+PRECISION_PLAIN = 0       # MPS_PRECISION_PLAIN
+PRECISION_MIXED = 1       # MPS_PRECISION_MIXED
 
 
 # (name, restype, argtypes) for every symbol the header declares.
@@ -71,6 +76,9 @@ SIGNATURES = {
     "mps_scale": (_I, [_P, _P, _SZ, ctypes.c_float, ctypes.c_float, _I]),
     "mps_cgemm": (_I, [_P, _I, _I, _I, _P, _LL, _LL, _I, _P, _LL, _LL, _I, _P, _LL, _LL, _I,
                        _LL, _LL, _LL]),
+    "mps_cgemm_tc": (_I, [_P, _I, _I, _I, _P, _LL, _LL, _I, _P, _LL, _LL, _I, _P, _LL, _LL, _I,
+                          _LL, _LL, _LL]),
+    "mps_tc_error": (_I, [_P]),
     "mps_marginals_workspace_bytes": (_SZ, [_P, _I, _I]),
     "mps_site_marginals": (_I, [_P, _P, _P, _I, _I, _P, _SZ, _P]),
 }

@@ -151,7 +151,20 @@ def _cgemm(lib, stream, m, n, k, a, a_off, sam, sak, conj_a, b, b_off, sbk, sbn,
             ctypes.c_void_p(c.data_ptr() + 8 * (c_off + z0 * bsc)), scm, scn, nb, bsa, bsb, bsc))
 
 
-def _given_svd(device, stream, mat, left_canonical: bool):
+def _check_svd_rc(rc: int, on_unconverged: str = "raise") -> None:
+    """Maps the two-qudit call's status to an exception.  A Jacobi SVD that hit
+    its sweep cap (MPS_ERR_NOT_CONVERGED) raises like any device error unless
+    the caller opted into ``on_unconverged="warn"``, which keeps the factors
+    of the last sweep and issues a RuntimeWarning instead."""
+    if rc == _native.MPS_OK:
+        return
+    if rc == _native.MPS_ERR_NOT_CONVERGED and on_unconverged == "warn":
+        warnings.warn("mpsim_gb300: " + _native.last_error(), RuntimeWarning)
+        return
+    raise _native.NativeError(rc, _native.last_error())
+
+
+def _given_svd(device, stream, mat, left_canonical: bool, on_unconverged: str = "raise"):
     """Thin SVD of a device matrix ``mat`` (m x n complex64, row-major) with
     the two-qudit kernel's given-matrix jobs (MPS_JOB_THETA_GIVEN, d = 1), keeping all
     r = min(m, n) values.  Returns (left (m, r), right (r, n), singular values
@@ -184,10 +197,7 @@ def _given_svd(device, stream, mat, left_canonical: bool):
     rc = lib.mps_apply_2q_batch(stream, ctypes.c_void_p(jobs.data_ptr()), 1, m, n, 1,
                                 ctypes.c_void_p(ws.data_ptr()), ws.numel(),
                                 ctypes.byref(_native.SvdParams()))
-    if rc == _native.MPS_ERR_NOT_CONVERGED:
-        warnings.warn("mpsim_gb300: " + _native.last_error(), RuntimeWarning)
-    elif rc != _native.MPS_OK:
-        raise _native.NativeError(rc, _native.last_error())
+    _check_svd_rc(rc, on_unconverged)
     return a_out.view(m, r), b_out.view(r, n), sv.cpu().numpy()[:r]
 
 
@@ -283,7 +293,8 @@ class MPS:
     """Matrix product state on one GPU (mpsim/core.py:159-1423)."""
 
     def __init__(self, nqudits: int, qudit_dimension: int = 2, tensor_prefix: str = "q",
-                 *, track_norms: bool = False, record_svals: bool = False) -> None:
+                 *, track_norms: bool = False, record_svals: bool = False,
+                 on_unconverged: str = "raise", precision: str = "plain") -> None:
         if nqudits < 2:
             raise ValueError(f"Number of qudits must be greater than 2 but is {nqudits}.")
         self._nqudits = int(nqudits)
@@ -295,6 +306,18 @@ class MPS:
         self.record_svals = record_svals
         self.svals_history = []
         self.svd_params = _native.SvdParams()
+        if on_unconverged not in ("raise", "warn"):
+            raise ValueError("on_unconverged must be 'raise' or 'warn'")
+        # a Jacobi SVD that hits its sweep cap raises NativeError (or, with
+        # "warn", keeps the last sweep's factors and warns)
+        self.on_unconverged = on_unconverged
+        if precision not in ("plain", "mixed"):
+            raise ValueError("precision must be 'plain' or 'mixed'")
+        # "plain": complex64 on FP32 SIMT throughout.  "mixed": the truncated
+        # SVDs of left-canonical tall gates of 64+ columns run as tensor-core
+        # block sweeps (split-bf16 tcgen05 Gram and rotation GEMMs, FP64
+        # off-diagonal test); every other gate runs the plain form.
+        self.precision = precision
         # When a list, each batched two-qudit launch appends
         # (jobs, max_m, max_n, sweeps, start_event, end_event).
         self.timing = None
@@ -717,7 +740,8 @@ class MPS:
         node = self._sites[i]
         cl, d, cr = (int(x) for x in node.shape)
         max_err = threshold * self.norm()
-        left, right, s = _given_svd(self._device, self._stream(), node.reshape(cl * d, cr), True)
+        left, right, s = _given_svd(self._device, self._stream(), node.reshape(cl * d, cr), True,
+                                     self.on_unconverged)
         keep = kept_by_truncation_error(s, max_err)
         r = int(left.shape[1])
         nxt = self._sites[i + 1]
@@ -740,7 +764,8 @@ class MPS:
         node = self._sites[i]
         cl, d, cr = (int(x) for x in node.shape)
         max_err = threshold * self.norm()
-        left, right, s = _given_svd(self._device, self._stream(), node.reshape(cl, d * cr), False)
+        left, right, s = _given_svd(self._device, self._stream(), node.reshape(cl, d * cr), False,
+                                     self.on_unconverged)
         keep = kept_by_truncation_error(s, max_err)
         r = int(left.shape[1])
         prev = self._sites[i - 1]
@@ -906,9 +931,28 @@ class MPS:
             self._norms.append(self.norm())
 
     def _run_pairs(self, pairs):
-        """One batched launch for two-qudit gates on disjoint adjacent pairs."""
+        """One batched launch for two-qudit gates on disjoint adjacent pairs
+        (two with precision="mixed": the gates the tensor-core sweeps take,
+        and the rest)."""
         if not pairs:
             return
+        if self.precision == "mixed":
+            d = self._qudit_dimension
+            tc, rest = [], []
+            for p in pairs:
+                chil = int(self._site_list[p[1]].shape[0])
+                chir = int(self._site_list[p[1] + 1].shape[2])
+                m, n = chil * d, chir * d
+                (tc if (p[3] and m >= n and n >= 64) else rest).append(p)
+            if tc:
+                self._run_pair_group(tc, _native.PRECISION_MIXED)
+            if rest:
+                self._run_pair_group(rest, _native.PRECISION_PLAIN)
+        else:
+            self._run_pair_group(pairs, _native.PRECISION_PLAIN)
+
+    def _run_pair_group(self, pairs, precision):
+        """One mps_apply_2q_batch call for gates on disjoint adjacent pairs."""
         d = self._qudit_dimension
         dev = self._device
         njobs = len(pairs)
@@ -954,6 +998,7 @@ class MPS:
         nbytes = lib.mps_2q_workspace_bytes(njobs, max_m, max_n, d)
         ws = _WS.get(dev, nbytes, "2q")
         timing = self.timing
+        self.svd_params.precision = precision
         if timing is not None:
             ev0 = torch.cuda.Event(enable_timing=True)
             ev1 = torch.cuda.Event(enable_timing=True)
@@ -964,10 +1009,7 @@ class MPS:
         if timing is not None:
             ev1.record(torch.cuda.current_stream(dev))
             timing.append((njobs, max_m, max_n, self.svd_params.sweeps_out, ev0, ev1))
-        if rc == _native.MPS_ERR_NOT_CONVERGED:
-            warnings.warn("mpsim_gb300: " + _native.last_error(), RuntimeWarning)
-        elif rc != _native.MPS_OK:
-            raise _native.NativeError(rc, _native.last_error())
+        _check_svd_rc(rc, self.on_unconverged)
         for left, a_out, b_out in outs:
             self._sites[left] = a_out
             self._version += 1
@@ -1158,7 +1200,8 @@ class MPS:
         new._norms = list(self._norms)
         new.svals_history = list(self.svals_history)
         new.svd_params = _native.SvdParams(self.svd_params.max_sweeps, self.svd_params.tol, 0, 0,
-                                           self.svd_params.wait_limit, 0)
+                                           self.svd_params.wait_limit, 0,
+                                           self.svd_params.precision)
         return new
 
     def __str__(self):

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <mutex>
 #include <string>
 
 #include "../../include/mpsim_gb300.h"
@@ -103,5 +104,18 @@ int cuda_fail(cudaError_t e, const char* what);
     } while (0)
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Devices a process may use with this library (per-device one-time setup).
+constexpr int kMaxDevices = 64;
+
+// One-time setup of a kernel on each device: the dynamic shared-memory
+// opt-in (cudaFuncAttributeMaxDynamicSharedMemorySize) is a per-device
+// attribute, and resident-CTA counts depend on the device.
+struct KernelSetup {
+    std::once_flag once[kMaxDevices];
+    int rc[kMaxDevices];
+    int limit[kMaxDevices];   // largest dynamic shared memory the kernel may request
+    int ctas[kMaxDevices];    // resident CTAs on the whole device (where computed)
+};
 
 }  // namespace mps

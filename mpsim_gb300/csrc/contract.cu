@@ -67,17 +67,59 @@ __global__ void apply_1q_kernel(cf* __restrict__ site, int chil, int d, int chir
     }
 }
 
-// Batched one-qudit gates: blockIdx.y selects the (site, gate) job.
+// Batched one-qudit gates: blockIdx.y selects the (site, gate) job.  A job
+// whose chi_r is even and whose site is 16-byte aligned (every torch
+// allocation is) runs the vectorised form: each thread owns two adjacent r
+// and moves them as one 16-byte load and store per a; the 128 threads of a
+// CTA form rows of rpw = next power of two of (chi_r / 2), capped at 128,
+// lanes, so (l, r) comes from shifts and masks, never from an integer divide.
+// Other jobs take the scalar form (one thread per (l, r)).
+constexpr int ONEQ_T = 128;
+
 template <int DMAX>
-__global__ void apply_1q_batch_kernel(const mps_1q_job* __restrict__ jobs, int d) {
+__global__ void __launch_bounds__(ONEQ_T) apply_1q_batch_kernel(const mps_1q_job* __restrict__ jobs,
+                                                                int d) {
     __shared__ cf U[DMAX * DMAX];
     const mps_1q_job job = jobs[blockIdx.y];
     const cf* gate = reinterpret_cast<const cf*>(job.gate);
     for (int e = threadIdx.x; e < d * d; e += blockDim.x) U[e] = gate[e];
     __syncthreads();
     const int chil = job.chi_l, chir = job.chi_r;
-    const size_t total = (size_t)chil * chir;
     cf* site = reinterpret_cast<cf*>(job.site);
+    if ((chir & 1) == 0 && (reinterpret_cast<uintptr_t>(site) & 15) == 0) {
+        const int rp = chir >> 1;                       // r pairs per row
+        int sh = 0;
+        while ((1 << sh) < rp && sh < 7) ++sh;          // rpw = 2^sh lanes per row
+        const int rows = ONEQ_T >> sh;                  // rows per pass of the CTA
+        const int ly = threadIdx.x >> sh, qx = threadIdx.x & ((1 << sh) - 1);
+        const size_t rs = (size_t)d * chir;             // complex per l row
+        for (int l = blockIdx.x * rows + ly; l < chil; l += gridDim.x * rows) {
+            float4* row = reinterpret_cast<float4*>(site + (size_t)l * rs);
+            for (int q = qx; q < rp; q += 1 << sh) {
+                float4 v[DMAX];
+#pragma unroll
+                for (int a = 0; a < DMAX; ++a)
+                    if (a < d) v[a] = __ldcs(row + (size_t)a * rp + q);
+#pragma unroll
+                for (int ap = 0; ap < DMAX; ++ap) {
+                    if (ap < d) {
+                        cf a0 = cmake(0.f, 0.f), a1 = cmake(0.f, 0.f);
+#pragma unroll
+                        for (int a = 0; a < DMAX; ++a) {
+                            if (a < d) {
+                                const cf u = U[ap * d + a];
+                                cfma(a0, u, cmake(v[a].x, v[a].y));
+                                cfma(a1, u, cmake(v[a].z, v[a].w));
+                            }
+                        }
+                        __stcs(row + (size_t)ap * rp + q, make_float4(a0.x, a0.y, a1.x, a1.y));
+                    }
+                }
+            }
+        }
+        return;
+    }
+    const size_t total = (size_t)chil * chir;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
          t += (size_t)gridDim.x * blockDim.x) {
         const size_t l = t / chir, r = t % chir;
@@ -288,12 +330,13 @@ extern "C" int mps_apply_1q_batch(void* stream, const mps_1q_job* jobs, int njob
     if (njobs == 0) return MPS_OK;
     if (njobs < 0 || njobs > 65535 || !jobs) return fail(MPS_ERR_ARG, "mps_apply_1q_batch: bad job list");
     if (d < 1 || d > 64) return fail(MPS_ERR_ARG, "mps_apply_1q_batch: bad qudit dimension");
-    dim3 grid(8, njobs);
-    if (d <= 2) apply_1q_batch_kernel<2><<<grid, 256, 0, s>>>(jobs, d);
-    else if (d <= 4) apply_1q_batch_kernel<4><<<grid, 256, 0, s>>>(jobs, d);
-    else if (d <= 8) apply_1q_batch_kernel<8><<<grid, 256, 0, s>>>(jobs, d);
-    else if (d <= 16) apply_1q_batch_kernel<16><<<grid, 256, 0, s>>>(jobs, d);
-    else apply_1q_batch_kernel<64><<<grid, 256, 0, s>>>(jobs, d);
+    // 16 CTAs per job: a 64-site chi=256 layer is 1024 CTAs, ~7 per SM
+    dim3 grid(16, njobs);
+    if (d <= 2) apply_1q_batch_kernel<2><<<grid, ONEQ_T, 0, s>>>(jobs, d);
+    else if (d <= 4) apply_1q_batch_kernel<4><<<grid, ONEQ_T, 0, s>>>(jobs, d);
+    else if (d <= 8) apply_1q_batch_kernel<8><<<grid, ONEQ_T, 0, s>>>(jobs, d);
+    else if (d <= 16) apply_1q_batch_kernel<16><<<grid, ONEQ_T, 0, s>>>(jobs, d);
+    else apply_1q_batch_kernel<64><<<grid, ONEQ_T, 0, s>>>(jobs, d);
     MPS_LAUNCH_CHECK("apply_1q_batch_kernel");
     return MPS_OK;
 }

@@ -48,87 +48,12 @@
 #include <mutex>
 #include <string>
 
+#include "rot.cuh"
 #include "twoq.cuh"
 
 namespace mps {
 
 namespace {
-
-// Squared cosine of the angle between two columns, |gamma|^2 / (a b).  A pair
-// rotates when it exceeds tol^2, and the per-job maximum of the same value
-// decides convergence, so a sweep that rotates nothing always ends the job.
-// Zero columns give 0; when g2 = |gamma|^2 or a norm is below the smallest
-// normal float, the cosine is formed from |gamma| and the square roots of the
-// norms with IEEE operations instead.
-__device__ __forceinline__ float pair_cos2(cf gam, float g2, float a, float b) {
-    const float kMinNormal = 1.17549435e-38f;
-    if (g2 >= kMinNormal && a >= kMinNormal && b >= kMinNormal)
-        return __fdividef(__fdividef(g2, a), b);
-    // |gamma|^2 underflows once the columns are below ~1e-10 in norm (graded
-    // columns, as the L factor has from the start): take |gamma| itself.
-    // Pairs with a + b below 1e-36 leave no room for the rotation's
-    // 1/(a+b) and count as orthogonal.
-    if (!(a > 0.f && b > 0.f) || !(a + b >= 1e-36f)) return 0.f;
-    const float r = (hypotf(gam.x, gam.y) / sqrtf(a)) / sqrtf(b);
-    return r * r;
-}
-
-// The rotation of a pair in the form
-//   x <- x - (tp x + sigma q),   q <- q + (conj(sigma) x - tp q),
-// sigma = s conj(gamma)/|gamma|, tp = 1 - c = s^2 / (1 + c): the complex
-// Jacobi rotation [[c, -sigma], [conj(sigma), c]], with c kept implicit as
-// 1 - tp (see the file comment).  It equals the rotation with the unit phase
-// e = conj(gamma)/|gamma| applied to q (q <- e q + ...) followed by conj(e)
-// on the new q, which changes no norm and no orthogonality.  dn = t |gamma|
-// is the norm transfer: |x'|^2 = a - dn, |q'|^2 = b + dn.
-struct Rot {
-    float tp, dn;
-    cf sigma;
-};
-
-// Rotation parameters for gamma != 0 from quantities scaled by u = 1/(a+b)
-// (gamma u is squared, not gamma: no overflow or underflow for a + b >= 1e-36):
-// t = sign(b-a) 2|gamma| / (|b-a| + sqrt((b-a)^2 + 4|gamma|^2)),
-// c = 1/sqrt(1+t^2) (approximate reciprocal square root refined by one
-// Newton step), s = c t.  |sigma|^2 and tp come from the same c^2 t^2, so
-// rounding perturbs a rotated column's norm by a few ulps times s^2 only.
-__device__ __forceinline__ Rot make_rot(float a, float b, cf gam) {
-    const float ab = a + b;
-    const float u = ab >= 1e-30f ? __fdividef(1.f, ab) : 1.f / ab;
-    const float p = b - a;
-    const float ph = p * u;                              // in [-1, 1]
-    const float gx = gam.x * u, gy = gam.y * u;
-    const float gh = fmaf(gx, gx, gy * gy);              // |gamma|^2 u^2, in (0, 1/4]
-    const float h = fmaf(ph, ph, 4.f * gh);
-    const float th = __fdividef(2.f, fabsf(ph) + h * rsqrtf(h));   // |t| / (|gamma| u)
-    const float t2 = gh * th * th;                       // t^2 <= 1
-    const float x = 1.f + t2;
-    float c = rsqrtf(x);
-    c = c * fmaf(-0.5f * x * c, c, 1.5f);                // Newton step for 1/sqrt(x)
-    const float sg = p >= 0.f ? 1.f : -1.f;
-    const float k = c * sg * u * th;                     // sigma = k conj(gamma)
-    Rot r;
-    r.sigma = cmake(k * gam.x, -k * gam.y);
-    r.tp = __fdividef(c * c * t2, 1.f + c);
-    r.dn = sg * gh * th * ab;                            // = sg |gamma|^2 u th
-    return r;
-}
-
-__device__ __forceinline__ void apply_rot(const Rot& r, cf& x, cf& q) {
-    const float sr = r.sigma.x, si = r.sigma.y, tp = r.tp;
-    float nxr = fmaf(-tp, x.x, x.x), nxi = fmaf(-tp, x.y, x.y);
-    float nqr = fmaf(-tp, q.x, q.x), nqi = fmaf(-tp, q.y, q.y);
-    nxr = fmaf(-sr, q.x, nxr);
-    nxi = fmaf(-sr, q.y, nxi);
-    nqr = fmaf(sr, x.x, nqr);
-    nqi = fmaf(sr, x.y, nqi);
-    nxr = fmaf(si, q.y, nxr);
-    nxi = fmaf(-si, q.x, nxi);
-    nqr = fmaf(si, x.y, nqr);
-    nqi = fmaf(-si, x.x, nqi);
-    x = cmake(nxr, nxi);
-    q = cmake(nqr, nqi);
-}
 
 struct JobShape {
     int m, n, L, C, nb;
@@ -1305,17 +1230,36 @@ int dynamic_smem_limit(K kernel, int* limit) {
     return MPS_OK;
 }
 
+// Sets the kernel's dynamic shared-memory opt-in to the device's limit, once
+// per device; with threads > 0 also counts the CTAs of (threads, smem) that
+// fit on the whole device.
 template <typename K>
-int prepare_kernel(K kernel, std::once_flag& once, int& limit, int& rc) {
-    std::call_once(once, [&] {
-        rc = dynamic_smem_limit(kernel, &limit);
+int prepare_kernel(K kernel, KernelSetup& ks, int* limit, int threads = 0, size_t smem = 0,
+                   int* ctas = nullptr) {
+    int dev = 0;
+    MPS_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(MPS_ERR_ARG, "device index beyond 63");
+    std::call_once(ks.once[dev], [&] {
+        ks.ctas[dev] = 0;
+        int rc = dynamic_smem_limit(kernel, &ks.limit[dev]);
         if (rc == MPS_OK) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 limit);
+                                                 ks.limit[dev]);
             if (e != cudaSuccess) rc = cuda_fail(e, "cudaFuncSetAttribute(jacobi visit)");
         }
+        if (rc == MPS_OK && threads > 0) {
+            int sms = 0, per_sm = 0;
+            cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+            if (e != cudaSuccess) rc = cuda_fail(e, "resident CTAs of the sweep kernel");
+            ks.ctas[dev] = sms * (per_sm > 0 ? per_sm : 1);
+        }
+        ks.rc[dev] = rc;
     });
-    return rc;
+    *limit = ks.limit[dev];
+    if (ctas) *ctas = ks.ctas[dev];
+    return ks.rc[dev];
 }
 
 template <int BC>
@@ -1335,17 +1279,17 @@ int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g
                  float tol2, int lw, cudaStream_t s) {
     dim3 grid(pairs, njobs);
     if (round == 0) {
-        static std::once_flag once;
-        static int limit = 0, rc = MPS_OK;
-        if (prepare_kernel(full_visit_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
+        static KernelSetup ks;
+        int limit = 0;
+        if (int rc = prepare_kernel(full_visit_kernel<BC, ROWS>, ks, &limit)) return rc;
         const size_t smem = full_smem<BC>(lw);
         if (smem > (size_t)limit) return fail(MPS_ERR_ARG, "jacobi: merged matrix too long for shared memory");
         full_visit_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol2);
         MPS_LAUNCH_CHECK("full_visit_kernel");
     } else {
-        static std::once_flag once;
-        static int limit = 0, rc = MPS_OK;
-        if (prepare_kernel(ring_visit_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
+        static KernelSetup ks;
+        int limit = 0;
+        if (int rc = prepare_kernel(ring_visit_kernel<BC, ROWS>, ks, &limit)) return rc;
         const size_t smem = ring_smem<BC>(lw);
         if (smem > (size_t)limit) return fail(MPS_ERR_ARG, "jacobi: merged matrix too long for shared memory");
         ring_visit_kernel<BC, ROWS><<<grid, BC * 32, smem, s>>>(jobs, g, round, tol2);
@@ -1357,19 +1301,11 @@ int launch_visit(const mps_2q_job* jobs, int njobs, int pairs, const TwoQGeom& g
 template <int BC, int ROWS>
 int launch_sweep(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const TwoQGeom& g,
                  float tol2, int lw, const SweepSync& sync, int tbase, cudaStream_t s) {
-    static std::once_flag once;
-    static int limit = 0, rc = MPS_OK, ctas = 0;
-    if (prepare_kernel(sweep_kernel<BC, ROWS>, once, limit, rc) != MPS_OK) return rc;
+    static KernelSetup ks;
     const size_t smem = ring_smem<BC>(lw);
+    int limit = 0, ctas = 0;
+    if (int rc = prepare_kernel(sweep_kernel<BC, ROWS>, ks, &limit, BC * 32, smem, &ctas)) return rc;
     if (smem > (size_t)limit) return fail(MPS_ERR_ARG, "jacobi: merged matrix too long for shared memory");
-    if (ctas == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        MPS_CUDA_CHECK(cudaGetDevice(&dev));
-        MPS_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        MPS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<BC, ROWS>,
-                                                                    BC * 32, smem));
-        ctas = sms * (per_sm > 0 ? per_sm : 1);
-    }
     const int items = rounds * njobs * pairs;
     const int grid = items < ctas ? items : ctas;
     if (grid <= 0) return MPS_OK;
@@ -1528,10 +1464,14 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     // backward-stable complex64 SVD gives.
     if (!(tol > 0.f)) tol = 5.9604645e-8f * fmaxf(8.f, sqrtf((float)lo.lslot));
     const float tol2 = tol * tol;     // the kernels compare squared cosines
+    const bool mixed = params && params->precision == MPS_PRECISION_MIXED;
+    if (params && params->precision != MPS_PRECISION_PLAIN && !mixed)
+        return fail(MPS_ERR_ARG, "mps_apply_2q_batch: unknown precision");
     const int lw = lo.lslot;
     int bc = 16;
     (void)pick_visit(lw, &bc);
     sweep_fn sweep = pick_sweep(lw);
+    if (mixed) bc = 32;
     if (params) params->block_cols = bc;
     SweepSync sync;
     sync.next_item = reinterpret_cast<int*>(ws + lo.off_sync);
@@ -1540,7 +1480,9 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     sync.nbmax = lo.nbmax;
     sync.wait_limit = (params && params->wait_limit > 0) ? params->wait_limit : (1 << 22);
     sync.stall_test = params ? params->stall_test : 0;
-
+    if (mixed && (lo.lslot % 64 != 0 || min(max_m, max_n) < 64))
+        return fail(MPS_ERR_ARG, "mps_apply_2q_batch: MPS_PRECISION_MIXED needs jobs of 64+ "
+                                 "columns");
     // padding rows and columns of X must be zero; no block has a stamp yet
     MPS_CUDA_CHECK(cudaMemsetAsync(g.X, 0, lo.off_V - lo.off_X, s));
     MPS_CUDA_CHECK(cudaMemsetAsync(g.vstamp, 0xff, lo.off_qst - lo.off_vst +
@@ -1567,7 +1509,7 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     const int rounds = nbmax - 1, pairs = nbmax / 2;
 
     if (!t_pinned) {
-        MPS_CUDA_CHECK(cudaHostAlloc(reinterpret_cast<void**>(&t_pinned), 4 * sizeof(int),
+        MPS_CUDA_CHECK(cudaHostAlloc(reinterpret_cast<void**>(&t_pinned), 8 * sizeof(int),
                                      cudaHostAllocDefault));
     }
     int npow2 = 1;
@@ -1578,27 +1520,51 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (cmax >= 2) {
         for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
             MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
-            if (cmax > 2 * bc) {
-                presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc,
-                                                                   sweeps * (rounds + 1));
-                MPS_LAUNCH_CHECK("presort_kernel");
+            if (mixed) {
+                // tensor-core block sweeps: no visit-skipping stamps
+                TwoQGeom gm = g;
+                gm.vstamp = nullptr;
+                gm.qstamp = nullptr;
+                if (cmax > 2 * bc) {
+                    presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, gm, npow2, bc, 0);
+                    MPS_LAUNCH_CHECK("presort_kernel");
+                }
+                rc = tc_sweep_launch(jobs, njobs, rounds, pairs, gm, tol2, s);
+                if (rc) return rc;
+            } else {
+                if (cmax > 2 * bc) {
+                    presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc,
+                                                                       sweeps * (rounds + 1));
+                    MPS_LAUNCH_CHECK("presort_kernel");
+                }
+                // one persistent launch runs every round of the sweep
+                MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, 2 * sizeof(int), s));
+                MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
+                                               (size_t)njobs * lo.nbmax * sizeof(int), s));
+                rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, sweeps * (rounds + 1), s);
+                if (rc) return rc;
             }
-            // one persistent launch runs every round of the sweep
-            MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, 2 * sizeof(int), s));
-            MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
-                                           (size_t)njobs * lo.nbmax * sizeof(int), s));
-            rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, sweeps * (rounds + 1), s);
-            if (rc) return rc;
             sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
             MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, 2 * sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
+            if (mixed)
+                MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 3, g.counter + 2, 2 * sizeof(int),
+                                               cudaMemcpyDeviceToHost, s));
             MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 2, sync.error, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
             MPS_CUDA_CHECK(cudaStreamSynchronize(s));
             if (t_pinned[2] != 0)
                 return fail(MPS_ERR_TIMEOUT, "mps_apply_2q_batch: a round-dependency wait inside the "
                                              "sweep kernel expired; results are invalid");
+            if (mixed) {
+                if (t_pinned[3] != 0)
+                    return fail(MPS_ERR_ARG, "mps_apply_2q_batch: MPS_PRECISION_MIXED takes only "
+                                             "left-canonical tall jobs of 64+ columns");
+                if (t_pinned[4] != 0)
+                    return fail(MPS_ERR_TIMEOUT, "mps_apply_2q_batch: a tensor-core MMA wait "
+                                                 "expired; results are invalid");
+            }
             if (t_pinned[0] == 0) {
                 converged = true;
                 break;
@@ -1680,7 +1646,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[MPS_NOALLOC_SCR
 namespace mps {
 namespace {
 
-constexpr int kMaxDevices = 64;
 std::once_flag g_noalloc_once[kMaxDevices];
 void* g_noalloc_ptr[kMaxDevices];
 cudaError_t g_noalloc_err[kMaxDevices];

@@ -344,14 +344,18 @@ int lq_precondition(const mps_2q_job* jobs, int njobs, int max_m, int max_n, con
                     cudaStream_t s) {
     const int cmax = min(min(max_m, max_n), LQ_MAX_C);
     if (cmax < LQ_MIN_C) return MPS_OK;
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
+    // the shared-memory opt-in is per device: set it once on every device used
+    static std::once_flag once[kMaxDevices];
+    static cudaError_t attr[kMaxDevices];
     const size_t smem_max = ((size_t)LQ_B * (LQ_MAX_C + 1) + 2 * LQ_B * LQ_B + 3 * LQ_B) * sizeof(cf);
-    std::call_once(once, [&] {
-        attr = cudaFuncSetAttribute(lq_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem_max);
+    int dev = 0;
+    MPS_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(MPS_ERR_ARG, "lq_precondition: device index beyond 63");
+    std::call_once(once[dev], [&] {
+        attr[dev] = cudaFuncSetAttribute(lq_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem_max);
     });
-    if (attr != cudaSuccess) return cuda_fail(attr, "cudaFuncSetAttribute(lq_panel_kernel)");
+    if (attr[dev] != cudaSuccess) return cuda_fail(attr[dev], "cudaFuncSetAttribute(lq_panel_kernel)");
     const size_t smem = ((size_t)LQ_B * (cmax + 1) + 2 * LQ_B * LQ_B + 3 * LQ_B) * sizeof(cf);
     for (int k0 = 0; k0 < cmax; k0 += LQ_B) {
         lq_panel_kernel<<<njobs, LQ_T, smem, s>>>(jobs, g, k0);

@@ -27,7 +27,7 @@ struct TwoQGeom {
     float* offmax;    // njobs: max relative off-diagonal seen this sweep
     int* done;        // njobs: 1 once a sweep made no rotation
     int* need;        // njobs: kept columns that need an orthonormal completion
-    int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf
+    int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf, [2] [3]: see tc_sweep_launch
     int* cmap;        // njobs * cslot: physical column at each sorted position
     float* cnrm;      // njobs * cslot: squared norm of each physical column
     int* scale;       // njobs: theta was multiplied by 2^scale[j] before the SVD
@@ -65,6 +65,12 @@ constexpr float kZeroSigma = 1e-30f;
 // from the final columns (lq.cu); the sweeps then need fewer passes.
 int lq_precondition(const mps_2q_job* jobs, int njobs, int max_m, int max_n, const TwoQGeom& g,
                     cudaStream_t s);
+
+// Tensor-core block sweeps (tcjacobi.cu): every round of one sweep of the
+// left-canonical tall jobs, 32-column blocks.  counter[2] is set when a job
+// of another kind was given, counter[3] when a bounded MMA wait expired.
+int tc_sweep_launch(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const TwoQGeom& g,
+                    float tol2, cudaStream_t s);
 
 int merge_gate_launch(const mps_2q_job* jobs, int njobs, int max_chil, int max_chir,
                       const TwoQGeom& g, cudaStream_t s);

@@ -1,7 +1,7 @@
 """Generate the golden fixtures under tests/golden/ (run once, in a container
 that has the reference checkout; the fixtures travel, the reference does not).
 
-  python tests/golden/make_golden.py [--reference /root/reference] [--only NAME]
+  python tests/golden/make_golden.py --reference PATH_TO_MPSIM_CHECKOUT [--only NAME]
 
 What it does:
 1. Puts ``oracle/tn_shim`` (a restatement of the TensorNetwork 0.2.1 subset the
@@ -349,7 +349,8 @@ def observables_fixture(core, tn):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True,
+                    help="root of a grmlarose/mpsim checkout (the directory holding mpsim/)")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     only = args.only
