@@ -35,9 +35,11 @@ extern "C" {
 #define MPS_ERR_NONFINITE 5    /* NaN/Inf met in a singular value           */
 #define MPS_ERR_TIMEOUT 6      /* a bounded in-kernel wait expired          */
 
-/* Per-job status bits written by mps_apply_2q_batch. */
+/* Per-job status bits written by mps_apply_2q_batch (the only report of a
+ * call made under stream capture, which reads nothing back). */
 #define MPS_STATUS_NOT_CONVERGED 1
 #define MPS_STATUS_NONFINITE 2
+#define MPS_STATUS_TIMEOUT 4
 
 typedef struct { float re, im; } mps_c64;
 
@@ -134,7 +136,11 @@ size_t mps_2q_workspace_bytes(int njobs, int max_m, int max_n, int d);
  * is then formed as U^H theta.  Blocks the calling thread
  * once per Jacobi sweep to test convergence, and returns after the last
  * sweep with the sort, regauge and output kernels still queued on the stream
- * (the outputs are stream-ordered like any kernel's).
+ * (the outputs are stream-ordered like any kernel's).  Under stream capture
+ * (cudaStreamIsCapturing) it never blocks: it queues params->max_sweeps
+ * sweeps (default 40; converged jobs return at once from each) and reports
+ * only through each job's status word, so a whole circuit can be captured
+ * into one CUDA graph.
  * Replaces MPS.apply_two_qudit_gate for adjacent sites (mpsim/core.py:
  * 1059-1152: merge 1059-1062, gate 1064-1068, truncated SVD 1132-1137 via
  * TensorNetwork split_node_full_svd, S placement 1139-1145). */
@@ -221,6 +227,11 @@ int mps_cgemm_tc(void* stream, int m, int n, int k, const mps_c64* a, long long 
 /* Reads and clears the flag the tensor-core kernels set when one of their
  * bounded mbarrier waits expired (their outputs are then invalid).  Blocks. */
 int mps_tc_error(int* flag_out);
+
+/* Profiling counters of the tensor-core Jacobi visits (MPS_PRECISION_MIXED):
+ * out4[0..2] = SM cycles summed over visits in the Gram, rotation-parameter
+ * and Y-update steps, out4[3] = visits, since the last reset.  Blocks. */
+int mps_tc_profile(unsigned long long* out4, int reset);
 
 /* Workspace for mps_site_marginals: every left environment plus two
  * right environments and two (chi, d, chi) scratch tensors. */

@@ -26,6 +26,7 @@ NOALLOC_SCRATCH_BYTES = 32 << 20       # MPS_NOALLOC_SCRATCH_BYTES
 
 STATUS_NOT_CONVERGED = 1
 STATUS_NONFINITE = 2
+STATUS_TIMEOUT = 4
 JOB_THETA_GIVEN = 1        # mps_2q_job.flags: a holds theta itself
 
 # mps_2q_job, field for field (88 bytes).
@@ -79,6 +80,7 @@ SIGNATURES = {
     "mps_cgemm_tc": (_I, [_P, _I, _I, _I, _P, _LL, _LL, _I, _P, _LL, _LL, _I, _P, _LL, _LL, _I,
                           _LL, _LL, _LL]),
     "mps_tc_error": (_I, [_P]),
+    "mps_tc_profile": (_I, [_P, _I]),
     "mps_marginals_workspace_bytes": (_SZ, [_P, _I, _I]),
     "mps_site_marginals": (_I, [_P, _P, _P, _I, _I, _P, _SZ, _P]),
 }

@@ -646,8 +646,11 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
     }
 }
 
-__global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol2) {
+__global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol2, const int* wait_error) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    // an expired round-dependency wait also marks every job's status (for
+    // calls that do not read the error word back: stream capture)
+    if (j == 0 && wait_error && *wait_error) atomicOr(g.counter + 3, 1);
     if (j >= njobs) return;
     if (!g.done[j]) {
         const float o = g.offmax[j];
@@ -827,6 +830,7 @@ sort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2) {
         g.need[j] = need;
         int st = 0;
         if (!g.done[j]) st |= MPS_STATUS_NOT_CONVERGED;
+        if (__ldcg(g.counter + 3)) st |= MPS_STATUS_TIMEOUT;
         if (s_bad) {
             st |= MPS_STATUS_NONFINITE;
             atomicAdd(g.counter + 1, 1);
@@ -1414,6 +1418,13 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
                                   size_t workspace_bytes, mps_svd_params* params) {
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (njobs == 0) return MPS_OK;
+    // Under stream capture (a CUDA graph) the call may not read anything back:
+    // it queues max_sweeps sweeps, in which converged jobs return at once, and
+    // leaves non-convergence, NaN/Inf and expired waits to the per-job status
+    // words (MPS_STATUS_*) for the caller to read after the replay.
+    cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+    MPS_CUDA_CHECK(cudaStreamIsCapturing(s, &cst));
+    const bool capturing = cst != cudaStreamCaptureStatusNone;
     if (njobs < 0 || njobs > 65535 || !jobs) return fail(MPS_ERR_ARG, "mps_apply_2q_batch: bad job list");
     if (d < 1 || d > 64) return fail(MPS_ERR_ARG, "mps_apply_2q_batch: qudit dimension must be 1..64");
     if (max_m <= 0 || max_n <= 0)
@@ -1508,7 +1519,7 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     nbmax += nbmax & 1;
     const int rounds = nbmax - 1, pairs = nbmax / 2;
 
-    if (!t_pinned) {
+    if (!t_pinned && !capturing) {
         MPS_CUDA_CHECK(cudaHostAlloc(reinterpret_cast<void**>(&t_pinned), 8 * sizeof(int),
                                      cudaHostAllocDefault));
     }
@@ -1521,7 +1532,9 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
             MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
             if (mixed) {
-                // tensor-core block sweeps: no visit-skipping stamps
+                // tensor-core block sweeps: no visit-skipping stamps and no
+                // round-dependency waits (sync.error stays 0)
+                if (sweeps == 1) MPS_CUDA_CHECK(cudaMemsetAsync(sync.error, 0, sizeof(int), s));
                 TwoQGeom gm = g;
                 gm.vstamp = nullptr;
                 gm.qstamp = nullptr;
@@ -1544,8 +1557,12 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
                 rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, sweeps * (rounds + 1), s);
                 if (rc) return rc;
             }
-            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2);
+            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2, sync.error);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
+            if (capturing) {
+                converged = true;            // reported through the status words
+                continue;
+            }
             MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, 2 * sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
             if (mixed)
@@ -1610,6 +1627,7 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     // call returns without waiting for its last kernels and the host can
     // prepare the next call meanwhile.  Jobs of one column have no sweep: read
     // the count here.
+    if (capturing) return MPS_OK;
     if (cmax < 2) {
         MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 1, g.counter + 1, sizeof(int),
                                        cudaMemcpyDeviceToHost, s));
@@ -1768,7 +1786,7 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
                 rc = visit(jobs, njobs, pairs, g, r, tol2, lw, s);
                 if (rc) return rc;
             }
-            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2);
+            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2, nullptr);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
             MPS_CUDA_CHECK(cudaMemcpyAsync(host_counter, g.counter, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));

@@ -133,20 +133,48 @@ def test_mixed_rejects_other_jobs(built_lib, cuda):
 
 def test_mixed_circuit_10q_matches_reference_complex128(built_lib, cuda):
     """The 10-qubit depth-10 untruncated workload with precision="mixed"
-    (its 64-column gates take the tensor-core sweeps): wavefunction
-    infidelity against the reference's complex128 run below 1e-5 (the plain
-    form reaches < 1e-9), amplitudes within 2e-6."""
+    (its merged matrices are at most 32 x 32, so every gate takes the plain
+    form): wavefunction infidelity against the reference's complex128 run
+    below 1e-9 and amplitudes within 2e-6 of its complex64 run, exactly the
+    plain form's bar."""
     from mpsim_gb300 import circuits as C
     from mpsim_gb300.core import MPS
     fx = np.load(os.path.join(GOLDEN, "brickwork_10q_d10_full.npz"))
     circ = C.workload("brickwork_10q_d10_full")
-    mps = MPS(circ.nqudits, circ.d, precision="mixed", record_svals=True)
+    mps = MPS(circ.nqudits, circ.d, precision="mixed")
     for lay in circ.layers:
         mps.apply_layer(lay.one_q, lay.pair_left, lay.two_q)
     got = mps.wavefunction().astype(np.complex128)
     ref = fx["ref_c128_wavefunction"]
     infid = 1.0 - abs(np.vdot(ref, got)) ** 2 / (np.vdot(ref, ref).real * np.vdot(got, got).real)
-    assert infid < 1e-5, infid
+    assert infid < 1e-9, infid
     assert np.allclose(got, fx["ref_c64_wavefunction"], atol=2e-6)
-    used = [c for c in mps.svals_history if len(c[0]) >= 64]
-    assert used, "no gate took the tensor-core sweeps"
+
+
+@pytest.mark.parametrize("nq,depth,d", [(14, 10, 2), (9, 8, 3)])
+def test_mixed_circuit_against_dense_fp64(built_lib, cuda, nq, depth, d):
+    """Untruncated brickwork circuits whose middle gates reach 64 to 128
+    columns (14 qubits; 9 qutrits) with precision="mixed", against the dense
+    complex128 evolution of the same gates: wavefunction infidelity <= 1e-5
+    (the precision form's target) and the plain form's result to 1e-6."""
+    from mpsim_gb300 import circuits as C
+    from mpsim_gb300.core import MPS
+    from oracle.dense import DenseState
+    circ = C.brickwork(nq, depth, d=d, maxsvals=None, seed=11)
+    mix = MPS(nq, d, precision="mixed", record_svals=True)
+    pln = MPS(nq, d)
+    st = DenseState(nq, d)
+    for lay in circ.layers:
+        mix.apply_layer(lay.one_q, lay.pair_left, lay.two_q)
+        pln.apply_layer(lay.one_q, lay.pair_left, lay.two_q)
+        for i in range(nq):
+            st.apply_one(lay.one_q[i], i)
+        for p, i in enumerate(lay.pair_left):
+            st.apply_two(lay.two_q[p], int(i), int(i) + 1)
+    ref = st.vector()
+    got = mix.wavefunction().astype(np.complex128)
+    infid = 1.0 - abs(np.vdot(ref, got)) ** 2 / (np.vdot(ref, ref).real * np.vdot(got, got).real)
+    assert infid <= 1e-5, infid
+    assert np.max(np.abs(got - pln.wavefunction())) < 1e-6 * max(1.0, np.max(np.abs(got)))
+    big = [h for h in mix.svals_history if len(h[0]) >= 64]
+    assert big, "no gate reached the tensor-core sweeps"
