@@ -626,6 +626,33 @@ def main():
     ops_ms = max_over_ranks(a0.elapsed_time(a1))
     ops_value = whole_job_rate(ngates, args.steps, world, ops_ms)
 
+    # the same circuit planned once (CircuitPlan: every table and buffer made
+    # before the first launch), run eagerly and replayed as one CUDA graph
+    from mpsim_gb300.plan import CircuitPlan
+    plan = CircuitPlan([circ], device=dev, precision=args.precision)
+    plan_state = plan.state(0)
+
+    def timed(fn):
+        fn()
+        barrier()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(args.steps):
+            flush.fill_(1)
+            fn()
+            plan_state.norm()
+        t1.record()
+        barrier()
+        return max_over_ranks(t0.elapsed_time(t1))
+
+    plan_ms = timed(plan.run)
+    plan_norm = plan_state.norm()
+    plan.capture()
+    graph_ms = timed(lambda: plan.replay(check=False))
+    plan.check_status()
+    graph_norm = plan_state.norm()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r, why = reference_rate(circ)
@@ -667,6 +694,12 @@ def main():
             "e2e_reference_api": {"value": ops_value, "unit": UNIT,
                                   "call": "MPS.apply([MPSOperation, ...], maxsvals=256) per layer, "
                                           "host gates, norm read back"},
+            "plan": {"value": whole_job_rate(ngates, args.steps, world, plan_ms), "unit": UNIT,
+                     "call": "CircuitPlan.run per step (all tables and buffers planned once), "
+                             "norm read back", "final_norm": plan_norm},
+            "graph": {"value": whole_job_rate(ngates, args.steps, world, graph_ms), "unit": UNIT,
+                      "call": "CircuitPlan captured as one CUDA graph, replayed per step, norm "
+                              "read back", "final_norm": graph_norm},
             "gpu_launches": int(launches),
             "clocks": clk,
             "final_norm": float(norms[-1]) if norms else None,

@@ -338,6 +338,19 @@ class MPS:
         init = init.to(self._device)
         self._site_list = [init[i].clone() for i in range(self._nqudits)]
 
+    @classmethod
+    def from_sites(cls, sites, qudit_dimension: int, **kwargs) -> "MPS":
+        """An MPS around existing device site tensors ((chi_l, d, chi_r)
+        complex64, shared, not copied), e.g. a CircuitPlan's final state."""
+        sites = list(sites)
+        mps = cls(len(sites), qudit_dimension, **kwargs)
+        for t in sites:
+            if t.dtype != torch.complex64 or t.dim() != 3 or int(t.shape[1]) != mps._qudit_dimension:
+                raise ValueError("sites must be (chi_l, d, chi_r) complex64 tensors")
+        mps._site_list = sites
+        mps._version += 1
+        return mps
+
     # -- deferred two-qudit gates ---------------------------------------------
     # apply_two_qudit_gate validates at once (the reference's exceptions) and
     # queues the gate; gates on disjoint adjacent pairs commute, so applying
