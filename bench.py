@@ -391,17 +391,60 @@ def circ_name(circ):
     return f"brickwork_{circ.nqudits}q_d{circ.depth}_chi{circ.maxsvals}"
 
 
+def batch_cpu_baseline(circs, states, budget_s=25.0):
+    """The complex128 oracle (the FP64 restatement of the reference's path) on
+    the cheapest circuits of the batch, as many as fit in ``budget_s``: its
+    rate (the CPU baseline of the batched form) and, per circuit, the
+    infidelity and norm error of the GPU state against it (MPS overlaps in
+    complex128).  ``states``: callables returning circuit i's GPU state."""
+    from oracle.ref_mps import OracleMPS, overlap_infidelity
+    from mpsim_gb300.circuits import estimated_cost
+    order = sorted(range(len(circs)), key=lambda i: estimated_cost(circs[i]))
+
+    def oracle(c, dtype):
+        o = OracleMPS(c.nqudits, c.d, dtype)
+        kw = {} if c.maxsvals is None else {"maxsvals": c.maxsvals}
+        for lay in c.layers:
+            for q in range(c.nqudits):
+                o.apply_one_qudit_gate(lay.one_q[q], q)
+            for p, j in enumerate(lay.pair_left):
+                o.apply_two_qudit_gate(lay.two_q[p], int(j), int(j) + 1, **kw)
+        return o
+
+    t0 = time.perf_counter()
+    t_c128, gates, errs = 0.0, 0, []
+    for i in order:
+        c = circs[i]
+        ta = time.perf_counter()
+        o = oracle(c, np.complex128)
+        t_c128 += time.perf_counter() - ta
+        gates += c.n_two_qudit_gates
+        o64 = oracle(c, np.complex64)
+        g = OracleMPS(c.nqudits, c.d, np.complex128)
+        g.sites = [t.detach().cpu().numpy().astype(np.complex128) for t in states(i).sites]
+        on, gn = o.norm(), g.norm()
+        errs.append({"circuit": i, "nqudits": c.nqudits, "depth": c.depth, "maxsvals": c.maxsvals,
+                     "infidelity": overlap_infidelity(o, g),
+                     "oracle_c64_infidelity": overlap_infidelity(o, o64),
+                     "norm_rel_err": abs(gn - on) / max(on, 1e-300)})
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return gates / t_c128, t_c128, errs
+
+
 def run_batch_workload(args, rank, world):
     """Multi-circuit workloads: batch_512_mixed and qutrit_128x32_d30_chi192.
-    A step is every circuit of the batch from |0...0> to its last layer.  With
-    several ranks the one batch is sharded by estimated cost
-    (circuits.shard_by_cost: circuits are independent, no collective on the
-    data path) and the step time is the slowest rank's: strong scaling."""
+    A step is every circuit of the batch from |0...0> to its last layer, run
+    as one CircuitPlan (all circuits advance together, one call per layer and
+    slot class) replayed as one CUDA graph.  With several ranks the batch is
+    sharded by estimated cost (circuits.shard_by_cost: circuits are
+    independent, no collective on the data path) and the step time is the
+    slowest rank's: strong scaling."""
     import torch
     import __graft_entry__ as ge
     from mpsim_gb300 import circuits as C
     from mpsim_gb300 import _native
-    from mpsim_gb300.batch import run_circuits
+    from mpsim_gb300.plan import CircuitPlan
 
     ge.build()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -426,46 +469,114 @@ def run_batch_workload(args, rank, world):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
-    for _ in range(args.warmup):
-        flush.fill_(1)
-        if circs:
-            run_circuits(circs)
-    barrier()
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(fn):
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            flush.fill_(1)
+            fn()
+        e1.record()
+        barrier()
+        return max_over_ranks(e0.elapsed_time(e1))
+
+    t_plan = time.perf_counter()
+    plan = CircuitPlan(circs, device=dev, precision=args.precision) if circs else None
+    plan_build_s = time.perf_counter() - t_plan
+    states = [plan.state(i) for i in range(len(circs))] if plan else []
+
+    def norms():
+        return [s.norm() for s in states]
+
+    for _ in range(max(args.warmup, 1)):
+        if plan:
+            plan.run()
+    eager_ms = timed(lambda: (plan.run(), norms()) if plan else None)
+    if plan:
+        plan.capture()
+        for _ in range(2):
+            plan.replay(check=False)
     clocks = Clocks(local)
     clocks.start()
     l0 = lib.mps_kernel_launches()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    states = []
-    for _ in range(args.steps):
-        flush.fill_(1)
-        if circs:
-            states = run_circuits(circs)
-    e1.record()
-    barrier()
+    graph_ms = timed(lambda: (plan.replay(check=False), norms()) if plan else None)
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    if plan:
+        plan.check_status()
+    # end to end through the public API: the plan built from the host
+    # circuits (gates and job tables copied in), run, norms read back
+    h2d = (plan.g1.numel() * 8 + plan.g2.numel() * 8 + plan.t1.numel() + plan.t2.numel()) if plan else 0
+    barrier()
+    w0 = time.perf_counter()
+    e2e_norms = []
+    for _ in range(args.steps):
+        if circs:
+            p2 = CircuitPlan(circs, device=dev, precision=args.precision)
+            p2.run()
+            e2e_norms = [p2.state(i).norm() for i in range(len(circs))]
+            del p2
+    barrier()
+    e2e_ms = max_over_ranks((time.perf_counter() - w0) * 1000.0)
     if rank == 0:
+        peaks, peak_kind = load_peaks()
+        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+        flops = 0.0
+        for c in every:
+            for (cl, cm, cr), count in C.gate_shapes(c)[1].items():
+                flops += count * gate_flops(cl * c.d, c.d * cr, cm, c.d)
+        achieved = flops * args.steps / (graph_ms / 1000.0) / 1e12
         line = {
             "metric": f"two-qudit gates/s ({args.workload})",
-            "value": ngates_all * args.steps / (ms / 1000.0),
+            "value": ngates_all * args.steps / (graph_ms / 1000.0),
             "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "ms_per_step": graph_ms / args.steps, "higher_is_better": True,
             "scaling": "strong" if world > 1 else "weak",
             "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded Haar gates)",
             "config": {"workload": args.workload, "circuits": len(every),
                        "two_qudit_gates_per_step": ngates_all,
+                       "precision": args.precision,
                        "parallelism": f"cost-sharded x{world}",
+                       "form": "CircuitPlan replayed as one CUDA graph",
                        "l2": "256 MiB buffer written at the start of every step"},
-            "circuits_per_s": len(every) * args.steps / (ms / 1000.0),
+            "circuits_per_s": len(every) * args.steps / (graph_ms / 1000.0),
+            "plan": {"value": ngates_all * args.steps / (eager_ms / 1000.0), "unit": UNIT,
+                     "call": "CircuitPlan.run per step (eager), norms read back",
+                     "build_s": plan_build_s},
+            "e2e": {"value": ngates_all * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 8 * len(every),
+                    "call": "CircuitPlan built from host circuits + run + norms, every step"},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "whole step (all launches), algorithmic flops of every gate",
+                         "peak_source": f"bf16 sustained ({peak_kind})"},
             "gpu_launches": int(lib.mps_kernel_launches() - l0), "clocks": clk,
-            "mean_norm": float(np.mean([s.norm() for s in states])) if states else None,
+            "mean_norm": float(np.mean(norms())) if states else None,
         }
+        if world == 1 and not args.no_cpu_baseline and circs:
+            rate, dt, errs = batch_cpu_baseline(circs, lambda i: states[i])
+            inf = [e["infidelity"] for e in errs]
+            line["cpu_baseline"] = {
+                "value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                "sample": f"complex128 NumPy oracle on the {len(errs)} cheapest circuits "
+                          f"({dt:.1f}s)"}
+            inf64 = [e["oracle_c64_infidelity"] for e in errs]
+            line["error_vs_fp64_oracle"] = {
+                "circuits": len(errs), "max_infidelity": max(inf),
+                "median_infidelity": float(np.median(inf)),
+                "max_norm_rel_err": max(e["norm_rel_err"] for e in errs),
+                "oracle_c64_max_infidelity": max(inf64),
+                "oracle_c64_median_infidelity": float(np.median(inf64)),
+                "note": "the complex64 oracle's own infidelity against complex128 on the same "
+                        "circuits: what truncated chaotic dynamics does to any complex64 run",
+                "worst_circuits": sorted(errs, key=lambda e: -e["infidelity"])[:10]}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -34,6 +34,27 @@ def gate_seed(base: int, instance: int, layer: int, slot: int, kind: int) -> int
     return int(ss.generate_state(1, dtype=np.uint32)[0])
 
 
+def gate_seeds(base: int, instance: int, layer: int, slots, kind: int) -> List[int]:
+    """gate_seed for many slots of one layer."""
+    return [gate_seed(base, instance, layer, int(i), kind) for i in slots]
+
+
+def haar_batch(nqudits: int, d: int, seeds: Sequence[int]) -> np.ndarray:
+    """haar_random_matrix(nqudits, d, seed) for every seed, stacked: the same
+    RandomState draws, one stacked QR (NumPy factorises each matrix with the
+    same LAPACK call as for a single one, so every gate is identical) and the
+    same phase fix."""
+    dim = d ** nqudits
+    if len(seeds) == 0:
+        return np.zeros((0, dim, dim), np.complex128)
+    z = np.stack([np.random.RandomState(s).randn(dim, dim, 2) for s in seeds])
+    mat = (z[..., 0] + 1j * z[..., 1]) / np.sqrt(2)
+    q, r = np.linalg.qr(mat)
+    ph = np.diagonal(r, axis1=1, axis2=2).copy()
+    ph /= np.abs(ph)
+    return q * ph[:, None, :]
+
+
 @dataclass
 class Layer:
     one_q: np.ndarray              # (n, d, d) complex128: U[a', a] per site
@@ -78,17 +99,23 @@ def brickwork(nqudits: int, depth: int, d: int = 2, maxsvals: Optional[int] = No
     cz = np.diag([1, 1, 1, -1]).astype(np.complex128)
     cn = _cnot_matrix.reshape(4, 4).astype(np.complex128)
     for t in range(depth):
-        one = np.stack([haar_random_matrix(1, d, gate_seed(seed, instance, t, i, KIND_1Q))
-                        for i in range(nqudits)])
+        one = haar_batch(1, d, gate_seeds(seed, instance, t, range(nqudits), KIND_1Q))
         start = t % 2
         lefts = np.arange(start, nqudits - 1, 2, dtype=np.int64)
-        twos = []
+        special = {}
         for i in lefts:
             if special_fraction > 0 and pick.random() < special_fraction:
-                twos.append(cn if pick.random() < 0.5 else cz)
+                special[int(i)] = cn if pick.random() < 0.5 else cz
+        haar_slots = [int(i) for i in lefts if int(i) not in special]
+        haar = haar_batch(2, d, gate_seeds(seed, instance, t, haar_slots, KIND_2Q))
+        two = np.zeros((len(lefts), d * d, d * d), np.complex128)
+        h = 0
+        for p, i in enumerate(lefts):
+            if int(i) in special:
+                two[p] = special[int(i)]
             else:
-                twos.append(haar_random_matrix(2, d, gate_seed(seed, instance, t, int(i), KIND_2Q)))
-        two = np.stack(twos) if twos else np.zeros((0, d * d, d * d), np.complex128)
+                two[p] = haar[h]
+                h += 1
         circ.layers.append(Layer(one, lefts, two))
     return circ
 
@@ -104,22 +131,44 @@ def workload(name: str, seed: int = 0, instance: int = 0) -> BrickworkCircuit:
     return brickwork(seed=seed, instance=instance, **WORKLOADS[name])
 
 
-def mixed_batch(ncircuits: int = 512, seed: int = 0) -> List[BrickworkCircuit]:
+def _brickwork_args(args):
+    return brickwork(*args[0], **args[1])
+
+
+def build_many(specs, workers: Optional[int] = None) -> List[BrickworkCircuit]:
+    """brickwork(*args, **kwargs) for every (args, kwargs) in ``specs``, spread
+    over the host cores (a spawn-context process pool: safe in a process
+    that already uses CUDA).  Drawing every gate from its own RandomState is
+    the cost (~0.15 ms a gate; ~160k gates in the 512-circuit batch)."""
+    import os
+    specs = list(specs)
+    workers = workers or min(len(specs), os.cpu_count() or 1, 32)
+    if workers <= 1 or len(specs) < 8:
+        return [_brickwork_args(s) for s in specs]
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_brickwork_args, specs, chunksize=max(1, len(specs) // (4 * workers))))
+
+
+def mixed_batch(ncircuits: int = 512, seed: int = 0, workers: Optional[int] = None
+                ) -> List[BrickworkCircuit]:
     """512 independent circuits: qubits U[16,48], depth U[8,32],
     maxsvals from {16,32,64,128}, 20% of two-qubit slots CNOT or CZ."""
-    out = []
+    specs = []
     for k in range(ncircuits):
         rng = np.random.default_rng(np.random.SeedSequence([seed, k, 104729]))
         nq = int(rng.integers(16, 49))
         depth = int(rng.integers(8, 33))
         chi = int(rng.choice([16, 32, 64, 128]))
-        out.append(brickwork(nq, depth, 2, chi, seed, k, special_fraction=0.2))
-    return out
+        specs.append(((nq, depth, 2, chi, seed, k), {"special_fraction": 0.2}))
+    return build_many(specs, workers)
 
 
-def qutrit_batch(ncircuits: int = 128, seed: int = 0) -> List[BrickworkCircuit]:
+def qutrit_batch(ncircuits: int = 128, seed: int = 0, workers: Optional[int] = None
+                 ) -> List[BrickworkCircuit]:
     """128 circuits of 32 qutrits, depth 30, maxsvals=192 (theta <= 576x576)."""
-    return [brickwork(32, 30, 3, 192, seed, k) for k in range(ncircuits)]
+    return build_many([((32, 30, 3, 192, seed, k), {}) for k in range(ncircuits)], workers)
 
 
 def gate_shapes(circ: BrickworkCircuit):

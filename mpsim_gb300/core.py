@@ -951,16 +951,30 @@ class MPS:
             return
         if self.precision == "mixed":
             d = self._qudit_dimension
-            tc, rest = [], []
-            for p in pairs:
+            tc, rest, tags_tc, tags_rest = [], [], [], []
+            for q, p in enumerate(pairs):
                 chil = int(self._site_list[p[1]].shape[0])
                 chir = int(self._site_list[p[1] + 1].shape[2])
                 m, n = chil * d, chir * d
-                (tc if (p[3] and m >= n and n >= 64) else rest).append(p)
+                if p[3] and m >= n and n >= 64:
+                    tc.append(p)
+                    tags_tc.append(q)
+                else:
+                    rest.append(p)
+                    tags_rest.append(q)
+            h0 = len(self.svals_history)
             if tc:
                 self._run_pair_group(tc, _native.PRECISION_MIXED)
             if rest:
                 self._run_pair_group(rest, _native.PRECISION_PLAIN)
+            if self.record_svals and tc and rest:
+                # keep the history in the order the gates were given
+                new = self.svals_history[h0:]
+                tags = tags_tc + tags_rest
+                ordered = [None] * len(tags)
+                for pos, q in enumerate(tags):
+                    ordered[q] = new[pos]
+                self.svals_history[h0:] = ordered
         else:
             self._run_pair_group(pairs, _native.PRECISION_PLAIN)
 
