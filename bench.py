@@ -47,10 +47,13 @@ def gate_flops(m, n, chim, d):
     return 8.0 * m * n * chim + 8.0 * m * n * d * d + 4.0 * (14.0 * big * small ** 2 + 8.0 * small ** 3)
 
 
-# DRAM bytes (read + write) of one mps_apply_2q_batch call on a chi=256 layer of
-# the default workload, summed over its 79 launches from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/traffic_2q_call_chi256.md).
-CALL_TRAFFIC_BYTES = 1.856e9
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of a chi=256
+# two-qudit call of 32 jobs, from one ncu capture per kernel (three launches
+# each, caches left warm) scaled by the launch counts of one call: per sweep
+# of the plain sweep kernel, and for the rest of the call (merge, LQ,
+# post-GEMMs, sorts).  A call's traffic is sweeps x the first + the second.
+SWEEP_TRAFFIC_BYTES = 1.12e9
+CALL_OTHER_TRAFFIC_BYTES = 1.16e9
 
 
 def replica_instance(rank: int) -> int:
@@ -583,6 +586,133 @@ def run_batch_workload(args, rank, world):
     return 0
 
 
+def run_case(args):
+    """Single-purpose chi=256 workloads for timing and profiling one kernel
+    family (``--case``), each run ``--steps`` times after ``--warmup`` runs,
+    timed with CUDA events on the launching stream after a 256 MiB buffer is
+    written (so L2 holds none of the case's data); one JSON line.
+
+      layer256        one mps_apply_2q_batch call: 32 jobs of theta 512 x 512
+                      (random sites, Haar gates), plain form
+      layer256_mixed  the same call in MPS_PRECISION_MIXED
+      onequbit256     one mps_apply_1q_batch over 64 sites of (256, 2, 256):
+                      HBM-bound, 2 x 64 x 1 MiB moved
+      norm256         MPS.norm of a 64-site chi=256 state (the overlap sweep)
+      tcgemm          mps_cgemm_tc, 1024 x 1024 x 1024 complex
+    """
+    import ctypes
+    import torch
+    import __graft_entry__ as ge
+    from mpsim_gb300 import _native
+    from mpsim_gb300.circuits import haar_random_matrix
+    from mpsim_gb300.core import MPS
+
+    ge.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lib = _native.load()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rng = np.random.default_rng(0)
+    d, chi = 2, 256
+
+    def rand_sites(n, cl, cr, scale):
+        t = rng.normal(size=(n, cl, d, cr)) + 1j * rng.normal(size=(n, cl, d, cr))
+        return torch.from_numpy((t * scale).astype(np.complex64)).to(dev)
+
+    keep = []
+    if args.case in ("layer256", "layer256_mixed"):
+        njobs = 32
+        A, B = rand_sites(njobs, chi, chi, 1.0 / chi), rand_sites(njobs, chi, chi, 1.0)
+        G = torch.from_numpy(np.stack([haar_random_matrix(2, d, 100 + q) for q in range(njobs)])
+                             .astype(np.complex64)).to(dev)
+        Ao = torch.empty((njobs, chi, d, chi), dtype=torch.complex64, device=dev)
+        Bo = torch.empty_like(Ao)
+        table = np.zeros(njobs, dtype=_native.JOB_DTYPE)
+        for q in range(njobs):
+            r = table[q]
+            r["a"], r["b"], r["gate"] = A[q].data_ptr(), B[q].data_ptr(), G[q].data_ptr()
+            r["a_out"], r["b_out"] = Ao[q].data_ptr(), Bo[q].data_ptr()
+            r["chi_l"], r["chi_m"], r["chi_r"], r["k"], r["keep_left_canonical"] = chi, chi, chi, chi, 1
+        jobs = torch.from_numpy(table.view(np.uint8)).to(dev)
+        nbytes = lib.mps_2q_workspace_bytes(njobs, 2 * chi, 2 * chi, d)
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        params = _native.SvdParams()
+        params.precision = (_native.PRECISION_MIXED if args.case == "layer256_mixed"
+                            else _native.PRECISION_PLAIN)
+
+        def once():
+            _native.check(lib.mps_apply_2q_batch(stream, ctypes.c_void_p(jobs.data_ptr()), njobs,
+                                                 2 * chi, 2 * chi, d, ctypes.c_void_p(ws.data_ptr()),
+                                                 nbytes, ctypes.byref(params)))
+        work = njobs * gate_flops(2 * chi, 2 * chi, chi, d) / 1e12
+        unit = "TFLOP/s (algorithmic, per call)"
+    elif args.case == "onequbit256":
+        nsite = 64
+        S = rand_sites(nsite, chi, chi, 1.0)
+        U = torch.from_numpy(np.stack([haar_random_matrix(1, d, q) for q in range(nsite)])
+                             .astype(np.complex64)).to(dev)
+        t1 = np.zeros(nsite, dtype=_native.JOB1_DTYPE)
+        for q in range(nsite):
+            t1[q]["site"], t1[q]["gate"] = S[q].data_ptr(), U[q].data_ptr()
+            t1[q]["chi_l"], t1[q]["chi_r"] = chi, chi
+        jt = torch.from_numpy(t1.view(np.uint8)).to(dev)
+
+        def once():
+            _native.check(lib.mps_apply_1q_batch(stream, ctypes.c_void_p(jt.data_ptr()), nsite, d))
+        work = 2 * S.numel() * 8 / 1e9
+        unit = "GB/s (site bytes read + written)"
+    elif args.case == "norm256":
+        n = 64
+        sites = []
+        for i in range(n):
+            cl = 1 if i == 0 else chi
+            cr = 1 if i == n - 1 else chi
+            sites.append(rand_sites(1, cl, cr, 1.0 / np.sqrt(cl * d))[0])
+        mps = MPS.from_sites(sites, d)
+
+        def once():
+            mps.norm()
+        work = sum(8.0 * d * t.shape[0] * t.shape[2] * (t.shape[0] + t.shape[2])
+                   for t in sites) / 1e12
+        unit = "TFLOP/s (overlap sweep, algorithmic)"
+    elif args.case == "tcgemm":
+        m = n = k = 1024
+        a, b = rand_sites(1, m, k // d, 1.0)[0], rand_sites(1, k, n // d, 1.0)[0]
+        c = torch.empty((m, n), dtype=torch.complex64, device=dev)
+
+        def once():
+            _native.check(lib.mps_cgemm_tc(stream, m, n, k, ctypes.c_void_p(a.data_ptr()), k, 1, 0,
+                                           ctypes.c_void_p(b.data_ptr()), n, 1, 0,
+                                           ctypes.c_void_p(c.data_ptr()), n, 1, 0, 0, 0, 0))
+        work = 8.0 * m * n * k / 1e12
+        unit = "TFLOP/s (complex 4M count)"
+    else:
+        raise SystemExit(f"unknown case {args.case}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        once()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1)                   # L2 (126 MB) holds nothing of the case
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        once()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    peaks, kind = load_peaks()
+    line = {"case": args.case, "ms_median": ms, "ms": times, "achieved": work / (ms / 1000.0),
+            "unit": unit, "launches_total": int(lib.mps_kernel_launches())}
+    if unit.startswith("GB/s"):
+        line["frac_of_hbm_copy"] = line["achieved"] / peaks["hbm_gbs"]
+        line["peak_source"] = f"hbm_gbs ({kind})"
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -593,11 +723,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncircuits", type=int, default=0)
     ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--case", default=None,
+                    choices=["layer256", "layer256_mixed", "onequbit256", "norm256", "tcgemm"],
+                    help="time one kernel family on a chi=256 case (for profiling)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.case:
+        return run_case(args)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     if args.workload in ("batch_512_mixed", "qutrit_128x32_d30_chi192"):
@@ -793,7 +928,9 @@ def main():
                        "l2": "256 MiB buffer written at the start of every step"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
-                         "traffic": CALL_TRAFFIC_BYTES if args.workload == WORKLOAD else None,
+                         "traffic": (mean_sweeps * SWEEP_TRAFFIC_BYTES + CALL_OTHER_TRAFFIC_BYTES
+                                     if (args.workload == WORKLOAD and mean_sweeps
+                                         and args.precision == "plain") else None),
                          "traffic_unit": "bytes per call (one chi=256 layer, 32 gates)",
                          "kernel": "mps_apply_2q_batch on chi=256 layers (merge + Jacobi SVD + "
                                    "regauge, all launches of one call)",

@@ -81,6 +81,10 @@ typedef struct {
                               expire (with a small wait_limit)             */
     int32_t precision;     /* MPS_PRECISION_PLAIN (default) or
                               MPS_PRECISION_MIXED                          */
+    int32_t lq_off;        /* nonzero: no LQ preconditioning (the sweeps run
+                              on theta itself)                              */
+    int32_t block_request; /* Jacobi block width of the plain form for slots
+                              of 512 / 576 rows: 0 (default) = 16, or 8     */
 } mps_svd_params;
 
 /* mps_svd_params.precision.

@@ -49,7 +49,8 @@ class SvdParams(ctypes.Structure):
     _fields_ = [("max_sweeps", ctypes.c_int32), ("tol", ctypes.c_float),
                 ("block_cols", ctypes.c_int32), ("sweeps_out", ctypes.c_int32),
                 ("wait_limit", ctypes.c_int32), ("stall_test", ctypes.c_int32),
-                ("precision", ctypes.c_int32)]
+                ("precision", ctypes.c_int32), ("lq_off", ctypes.c_int32),
+                ("block_request", ctypes.c_int32)]
 
 
 PRECISION_PLAIN = 0       # MPS_PRECISION_PLAIN

@@ -42,7 +42,7 @@ from typing import List, Optional, Sequence, Tuple, Union
 
 import numpy as np
 
-from . import _native
+from . import _native, autotune
 from .gates import (Node, cnot, gate_tensor, haar_random_unitary, hgate, is_hermitian,
                     is_unitary, rgate, swap, xgate)
 
@@ -294,7 +294,8 @@ class MPS:
 
     def __init__(self, nqudits: int, qudit_dimension: int = 2, tensor_prefix: str = "q",
                  *, track_norms: bool = False, record_svals: bool = False,
-                 on_unconverged: str = "raise", precision: str = "plain") -> None:
+                 on_unconverged: str = "raise", precision: str = "plain",
+                 autotune: bool = True) -> None:
         if nqudits < 2:
             raise ValueError(f"Number of qudits must be greater than 2 but is {nqudits}.")
         self._nqudits = int(nqudits)
@@ -311,13 +312,18 @@ class MPS:
         # a Jacobi SVD that hits its sweep cap raises NativeError (or, with
         # "warn", keeps the last sweep's factors and warns)
         self.on_unconverged = on_unconverged
-        if precision not in ("plain", "mixed"):
-            raise ValueError("precision must be 'plain' or 'mixed'")
+        if precision not in ("plain", "mixed", "auto"):
+            raise ValueError("precision must be 'plain', 'mixed' or 'auto'")
         # "plain": complex64 on FP32 SIMT throughout.  "mixed": the truncated
         # SVDs of left-canonical tall gates of 64+ columns run as tensor-core
         # block sweeps (split-bf16 tcgen05 Gram and rotation GEMMs, FP64
-        # off-diagonal test); every other gate runs the plain form.
+        # off-diagonal test); every other gate runs the plain form.  "auto":
+        # for those gates, whichever of the two the autotuner's table found
+        # faster for the call's shape and batch.
         self.precision = precision
+        # per-call solver settings (LQ preconditioning, block width) from the
+        # autotuner's table (mpsim_gb300.autotune); False keeps the defaults
+        self.autotune = autotune
         # When a list, each batched two-qudit launch appends
         # (jobs, max_m, max_n, sweeps, start_event, end_event).
         self.timing = None
@@ -949,7 +955,7 @@ class MPS:
         and the rest)."""
         if not pairs:
             return
-        if self.precision == "mixed":
+        if self.precision in ("mixed", "auto"):
             d = self._qudit_dimension
             tc, rest, tags_tc, tags_rest = [], [], [], []
             for q, p in enumerate(pairs):
@@ -963,6 +969,12 @@ class MPS:
                     rest.append(p)
                     tags_rest.append(q)
             h0 = len(self.svals_history)
+            if tc and self.precision == "auto":
+                mm = max(int(self._site_list[p[1]].shape[0]) * d for p in tc)
+                nn = max(int(self._site_list[p[1] + 1].shape[2]) * d for p in tc)
+                if autotune.lookup(mm, nn, d, len(tc))["precision"] != "mixed":
+                    rest, tags_rest = tc + rest, tags_tc + tags_rest
+                    tc, tags_tc = [], []
             if tc:
                 self._run_pair_group(tc, _native.PRECISION_MIXED)
             if rest:
@@ -1026,6 +1038,9 @@ class MPS:
         ws = _WS.get(dev, nbytes, "2q")
         timing = self.timing
         self.svd_params.precision = precision
+        tuned = autotune.lookup(max_m, max_n, d, njobs) if self.autotune else autotune.DEFAULT
+        self.svd_params.lq_off = tuned["lq_off"]
+        self.svd_params.block_request = tuned["block_request"] if precision == 0 else 0
         if timing is not None:
             ev0 = torch.cuda.Event(enable_timing=True)
             ev1 = torch.cuda.Event(enable_timing=True)
@@ -1228,7 +1243,8 @@ class MPS:
         new.svals_history = list(self.svals_history)
         new.svd_params = _native.SvdParams(self.svd_params.max_sweeps, self.svd_params.tol, 0, 0,
                                            self.svd_params.wait_limit, 0,
-                                           self.svd_params.precision)
+                                           self.svd_params.precision, self.svd_params.lq_off,
+                                           self.svd_params.block_request)
         return new
 
     def __str__(self):

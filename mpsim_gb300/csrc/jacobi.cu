@@ -1322,7 +1322,9 @@ int launch_sweep(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const
 typedef int (*sweep_fn)(const mps_2q_job*, int, int, int, const TwoQGeom&, float, int,
                         const SweepSync&, int, cudaStream_t);
 
-sweep_fn pick_sweep(int lw) {
+sweep_fn pick_sweep(int lw, int block_request) {
+    if (block_request == 8 && lw > 256 && lw <= 576)
+        return lw <= 512 ? launch_sweep<8, 16> : launch_sweep<8, 18>;
     if (lw <= 576) {
         if (lw <= 64) return launch_sweep<16, 2>;
         if (lw <= 128) return launch_sweep<16, 4>;
@@ -1481,7 +1483,11 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     const int lw = lo.lslot;
     int bc = 16;
     (void)pick_visit(lw, &bc);
-    sweep_fn sweep = pick_sweep(lw);
+    const int block_request = params ? params->block_request : 0;
+    if (block_request != 0 && block_request != 8 && block_request != 16)
+        return fail(MPS_ERR_ARG, "mps_apply_2q_batch: block_request must be 0, 8 or 16");
+    sweep_fn sweep = pick_sweep(lw, block_request);
+    if (block_request == 8 && lw > 256 && lw <= 576) bc = 8;
     if (mixed) bc = 32;
     if (params) params->block_cols = bc;
     SweepSync sync;
@@ -1510,7 +1516,7 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (rc) return rc;
     rc = scale_theta(jobs, njobs, g, s);
     if (rc) return rc;
-    rc = lq_precondition(jobs, njobs, max_m, max_n, g, s);
+    if (!(params && params->lq_off)) rc = lq_precondition(jobs, njobs, max_m, max_n, g, s);
     if (rc) return rc;
 
     const int cmax = min(max_m, max_n);

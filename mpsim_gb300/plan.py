@@ -39,6 +39,7 @@ import numpy as np
 import torch
 
 from . import _native
+from . import autotune as _autotune
 from .core import MPS, kept_count
 
 # padded merged-matrix lengths of the two-qudit kernel's slot classes
@@ -66,11 +67,11 @@ class CircuitPlan:
     d), ``pair_left`` and ``two_q`` (p, d^2, d^2)), e.g. ``circuits.brickwork``."""
 
     def __init__(self, circuits: Sequence, device=None, precision: str = "plain",
-                 keep_left_canonical: bool = True, max_sweeps: int = 40):
+                 keep_left_canonical: bool = True, max_sweeps: int = 40, autotune: bool = True):
         if not circuits:
             raise ValueError("CircuitPlan needs at least one circuit")
-        if precision not in ("plain", "mixed"):
-            raise ValueError("precision must be 'plain' or 'mixed'")
+        if precision not in ("plain", "mixed", "auto"):
+            raise ValueError("precision must be 'plain', 'mixed' or 'auto'")
         d = int(circuits[0].d)
         if any(int(c.d) != d for c in circuits):
             raise ValueError("all circuits of a plan must share the qudit dimension")
@@ -183,7 +184,8 @@ class CircuitPlan:
             for ci, i, p, chil, chim, chir, k in events[t]:
                 m, n = chil * d, chir * d
                 prec = (_native.PRECISION_MIXED
-                        if precision == "mixed" and _tc_eligible(m, n, lc) else _native.PRECISION_PLAIN)
+                        if precision in ("mixed", "auto") and _tc_eligible(m, n, lc)
+                        else _native.PRECISION_PLAIN)
                 oa, ob = cur[ci][i][0], cur[ci][i + 1][0]
                 wa, wb = which[ci][i], which[ci][i + 1]
                 na, nbo = buf_off[ci][i][wa], buf_off[ci][i + 1][wb]
@@ -195,13 +197,24 @@ class CircuitPlan:
                        status_n, chil, chim, chir, k, 1 if lc else 0, 0)
                 status_n += 1
                 groups.setdefault((prec, slot_class(m, n)), []).append((row, m, n))
+            if precision == "auto":
+                # mixed-eligible groups the tuner found faster in the plain form
+                for (prec, cls) in [g for g in groups if g[0] == _native.PRECISION_MIXED]:
+                    items = groups[(prec, cls)]
+                    mm, nn = max(x[1] for x in items), max(x[2] for x in items)
+                    if _autotune.lookup(mm, nn, d, len(items))["precision"] != "mixed":
+                        groups.setdefault((_native.PRECISION_PLAIN, cls), []).extend(
+                            groups.pop((prec, cls)))
             for (prec, _cls), items in sorted(groups.items()):
                 for a in range(0, len(items), _CHUNK):
                     part = items[a:a + _CHUNK]
                     lo2 = len(rows2)
                     rows2.extend(r for r, _, _ in part)
-                    calls.append(("2q", lo2, len(part), max(m for _, m, _ in part),
-                                  max(n for _, _, n in part), prec))
+                    mm, nn = max(m for _, m, _ in part), max(n for _, _, n in part)
+                    tuned = (_autotune.lookup(mm, nn, d, len(part)) if autotune
+                             else _autotune.DEFAULT)
+                    calls.append(("2q", lo2, len(part), mm, nn, prec, tuned["lq_off"],
+                                  tuned["block_request"] if prec == _native.PRECISION_PLAIN else 0))
         self.n_two_qudit_gates = status_n
         self.status = torch.zeros(max(status_n, 1), dtype=torch.int32, device=self.device)
         sp = self.status.data_ptr()
@@ -254,8 +267,9 @@ class CircuitPlan:
                 _native.check(lib.mps_apply_1q_batch(
                     stream, ctypes.c_void_p(j1 + cl[1] * _native.JOB1_DTYPE.itemsize), cl[2], d))
                 continue
-            _, lo, n, max_m, max_n, prec = cl
+            _, lo, n, max_m, max_n, prec, lq_off, block = cl
             p.precision = prec
+            p.lq_off, p.block_request = lq_off, block
             p.max_sweeps = self.max_sweeps
             if capturing and self.sweeps[ci] is not None:
                 p.max_sweeps = min(self.max_sweeps, self.sweeps[ci] + self.sweep_margin)
