@@ -93,26 +93,43 @@ __global__ void __launch_bounds__(ONEQ_T) apply_1q_batch_kernel(const mps_1q_job
         const int rows = ONEQ_T >> sh;                  // rows per pass of the CTA
         const int ly = threadIdx.x >> sh, qx = threadIdx.x & ((1 << sh) - 1);
         const size_t rs = (size_t)d * chir;             // complex per l row
-        for (int l = blockIdx.x * rows + ly; l < chil; l += gridDim.x * rows) {
+        const int step = gridDim.x * rows;
+        // two rows per iteration, every load issued before any arithmetic:
+        // 2 d 16-byte loads in flight per thread (the kernel is bound by
+        // load latency, not by instructions)
+        for (int l = blockIdx.x * rows + ly; l < chil; l += 2 * step) {
+            const int l2 = l + step;
+            const bool two = l2 < chil;
             float4* row = reinterpret_cast<float4*>(site + (size_t)l * rs);
+            float4* row2 = reinterpret_cast<float4*>(site + (size_t)(two ? l2 : l) * rs);
             for (int q = qx; q < rp; q += 1 << sh) {
-                float4 v[DMAX];
+                float4 v[DMAX], w[DMAX];
 #pragma unroll
-                for (int a = 0; a < DMAX; ++a)
-                    if (a < d) v[a] = __ldcs(row + (size_t)a * rp + q);
+                for (int a = 0; a < DMAX; ++a) {
+                    if (a < d) {
+                        v[a] = __ldcs(row + (size_t)a * rp + q);
+                        if (two) w[a] = __ldcs(row2 + (size_t)a * rp + q);
+                    }
+                }
 #pragma unroll
                 for (int ap = 0; ap < DMAX; ++ap) {
                     if (ap < d) {
                         cf a0 = cmake(0.f, 0.f), a1 = cmake(0.f, 0.f);
+                        cf b0 = cmake(0.f, 0.f), b1 = cmake(0.f, 0.f);
 #pragma unroll
                         for (int a = 0; a < DMAX; ++a) {
                             if (a < d) {
                                 const cf u = U[ap * d + a];
                                 cfma(a0, u, cmake(v[a].x, v[a].y));
                                 cfma(a1, u, cmake(v[a].z, v[a].w));
+                                if (two) {
+                                    cfma(b0, u, cmake(w[a].x, w[a].y));
+                                    cfma(b1, u, cmake(w[a].z, w[a].w));
+                                }
                             }
                         }
                         __stcs(row + (size_t)ap * rp + q, make_float4(a0.x, a0.y, a1.x, a1.y));
+                        if (two) __stcs(row2 + (size_t)ap * rp + q, make_float4(b0.x, b0.y, b1.x, b1.y));
                     }
                 }
             }
@@ -330,7 +347,9 @@ extern "C" int mps_apply_1q_batch(void* stream, const mps_1q_job* jobs, int njob
     if (njobs == 0) return MPS_OK;
     if (njobs < 0 || njobs > 65535 || !jobs) return fail(MPS_ERR_ARG, "mps_apply_1q_batch: bad job list");
     if (d < 1 || d > 64) return fail(MPS_ERR_ARG, "mps_apply_1q_batch: bad qudit dimension");
-    // 16 CTAs per job: a 64-site chi=256 layer is 1024 CTAs, ~7 per SM
+    // 16 CTAs per job, two rows per thread per iteration: a 64-site chi=256
+    // layer is 1024 CTAs of 128 threads, ~27 warps and ~55 KB of loads in
+    // flight per SM
     dim3 grid(16, njobs);
     if (d <= 2) apply_1q_batch_kernel<2><<<grid, ONEQ_T, 0, s>>>(jobs, d);
     else if (d <= 4) apply_1q_batch_kernel<4><<<grid, ONEQ_T, 0, s>>>(jobs, d);
