@@ -166,7 +166,9 @@ int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs_dev, int njobs,
  * jobs fit per call).  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress) with that device current: make it before any
  * stream capture.  Calls share the array: calls that overlap on the GPU race
- * and must be serialised by the caller. */
+ * and must be serialised by the caller.  The call returns only when its work
+ * on the stream has finished: it reads the convergence and non-finite counts
+ * back into host memory (always the plain form, whatever params->precision). */
 int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs_dev, int njobs,
                                int max_m, int max_n, int d, mps_svd_params* params);
 
