@@ -634,7 +634,7 @@ def run_case(args):
             r["a_out"], r["b_out"] = Ao[q].data_ptr(), Bo[q].data_ptr()
             r["chi_l"], r["chi_m"], r["chi_r"], r["k"], r["keep_left_canonical"] = chi, chi, chi, chi, 1
         jobs = torch.from_numpy(table.view(np.uint8)).to(dev)
-        nbytes = lib.mps_2q_workspace_bytes(njobs, 2 * chi, 2 * chi, d)
+        nbytes = lib.mps_2q_workspace_bytes_mixed(njobs, 2 * chi, 2 * chi, d)
         ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
         params = _native.SvdParams()
         params.precision = (_native.PRECISION_MIXED if args.case == "layer256_mixed"
@@ -709,6 +709,26 @@ def run_case(args):
     if unit.startswith("GB/s"):
         line["frac_of_hbm_copy"] = line["achieved"] / peaks["hbm_gbs"]
         line["peak_source"] = f"hbm_gbs ({kind})"
+    if args.case in ("layer256", "layer256_mixed"):
+        line["sweeps"] = int(params.sweeps_out)
+    if args.case == "layer256_mixed":
+        # cycles of the tensor-core visits per step (one more call, counters
+        # reset before it): Gram, rotations on G, update; and the visit count
+        cyc = (ctypes.c_ulonglong * 10)()
+        _native.check(lib.mps_tc_profile(cyc, 1))
+        once()
+        torch.cuda.synchronize()
+        _native.check(lib.mps_tc_profile(cyc, 1))
+        nv = max(int(cyc[3]), 1)
+        line["tc_visits"] = int(cyc[3])
+        line["tc_visits_rotating"] = int(cyc[4])
+        line["tc_rotating_steps_per_rotating_visit"] = cyc[5] / max(int(cyc[4]), 1)
+        line["tc_pairs_per_rotating_step"] = cyc[6] / max(int(cyc[5]), 1)
+        line["tc_wait_cycles_per_visit"] = cyc[7] / nv
+        line["tc_ctas_per_sweep"] = cyc[9] / max(int(params.sweeps_out), 1)
+        line["tc_cta_lifetime_cycles"] = cyc[8] / max(int(cyc[9]), 1)
+        line["tc_cycles_per_visit"] = {"gram": cyc[0] / nv, "rotations": cyc[1] / nv,
+                                       "update": cyc[2] / nv}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -128,6 +128,12 @@ int mps_apply_1q_batch(void* stream, const mps_1q_job* jobs_dev, int njobs, int 
  * matrices are at most max_m x max_n (m = chi_l*d, n = d*chi_r). */
 size_t mps_2q_workspace_bytes(int njobs, int max_m, int max_n, int d);
 
+/* The same for a call with params->precision == MPS_PRECISION_MIXED, whose
+ * workspace also holds every job's matrix split into three bf16 piece planes
+ * (12 more bytes per complex element); such a call with a smaller workspace
+ * returns MPS_ERR_WORKSPACE. */
+size_t mps_2q_workspace_bytes_mixed(int njobs, int max_m, int max_n, int d);
+
 /* Applies njobs independent two-qudit gates (jobs_dev: a device array of
  * mps_2q_job; the sites of different jobs must not alias).  Per job: merge
  * A.B with the gate fused in (theta = (chi_l*d) x (d*chi_r)), block one-sided
@@ -234,10 +240,14 @@ int mps_cgemm_tc(void* stream, int m, int n, int k, const mps_c64* a, long long 
  * bounded mbarrier waits expired (their outputs are then invalid).  Blocks. */
 int mps_tc_error(int* flag_out);
 
-/* Profiling counters of the tensor-core Jacobi visits (MPS_PRECISION_MIXED):
- * out4[0..2] = SM cycles summed over visits in the Gram, rotation-parameter
- * and Y-update steps, out4[3] = visits, since the last reset.  Blocks. */
-int mps_tc_profile(unsigned long long* out4, int reset);
+/* Profiling counters of the tensor-core Jacobi visits (MPS_PRECISION_MIXED),
+ * since the last reset: out10[0..2] = SM cycles summed over visits in the
+ * Gram, rotation and Y-update steps, out10[3] = visits, out10[4] = visits
+ * that rotated, out10[5] = inner steps that rotated, out10[6] = pairs
+ * rotated, out10[7] = cycles visits waited for their blocks' previous round,
+ * out10[8] = summed lifetimes of the sweep kernel's CTAs, out10[9] = those
+ * CTAs.  Blocks. */
+int mps_tc_profile(unsigned long long* out10, int reset);
 
 /* Workspace for mps_site_marginals: every left environment plus two
  * right environments and two (chi, d, chi) scratch tensors. */

@@ -69,6 +69,7 @@ SIGNATURES = {
     "mps_apply_1q": (_I, [_P, _P, _I, _I, _I, _P]),
     "mps_apply_1q_batch": (_I, [_P, _P, _I, _I]),
     "mps_2q_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
+    "mps_2q_workspace_bytes_mixed": (_SZ, [_I, _I, _I, _I]),
     "mps_apply_2q_batch": (_I, [_P, _P, _I, _I, _I, _I, _P, _SZ, ctypes.POINTER(SvdParams)]),
     "mps_apply_2q_batch_noalloc": (_I, [_P, _P, _I, _I, _I, _I, ctypes.POINTER(SvdParams)]),
     "mps_sweep_workspace_bytes": (_SZ, [_I, _I]),

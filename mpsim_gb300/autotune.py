@@ -150,7 +150,7 @@ def tune(shapes, njobs_list=(8, 32, 512), reps: int = 3, device=None, log=print)
         m, n = chil * d, chir * d
         for nj in njobs_list:
             keep, S = _jobs(device, chil, chim, chir, d, nj, 1000 + chil)
-            ws = torch.empty(lib.mps_2q_workspace_bytes(nj, m, n, d), dtype=torch.uint8,
+            ws = torch.empty(lib.mps_2q_workspace_bytes_mixed(nj, m, n, d), dtype=torch.uint8,
                              device=device)
             ref_ms, ref = _time(lib, keep, S, nj, m, n, d, ("plain", 0, 0), reps, ws)
             best, best_ms, res = ("plain", 0, 0), ref_ms, {}

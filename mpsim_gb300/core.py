@@ -1034,8 +1034,9 @@ class MPS:
             row["keep_left_canonical"] = 1 if lc else 0
         jobs = torch.from_numpy(table.view(np.uint8)).to(dev)
         lib = self._lib()
-        nbytes = lib.mps_2q_workspace_bytes(njobs, max_m, max_n, d)
-        ws = _WS.get(dev, nbytes, "2q")
+        size_fn = (lib.mps_2q_workspace_bytes_mixed if precision == _native.PRECISION_MIXED
+                   else lib.mps_2q_workspace_bytes)
+        ws = _WS.get(dev, size_fn(njobs, max_m, max_n, d), "2q")
         timing = self.timing
         self.svd_params.precision = precision
         tuned = autotune.lookup(max_m, max_n, d, njobs) if self.autotune else autotune.DEFAULT

@@ -1356,7 +1356,7 @@ visit_fn pick_visit(int lw, int* bc) {
 struct Layout {
     int lslot, cslot;
     size_t off_X, off_V, off_T, off_sig, off_perm, off_cmap, off_cnrm, off_off, off_done, off_need,
-        off_counter, off_scale, off_nrm2, off_sync, off_vst, off_qst, total;
+        off_counter, off_scale, off_nrm2, off_sync, off_vst, off_qst, off_P, total;
     int nbmax, qstride;
 };
 
@@ -1369,7 +1369,7 @@ int slot_rows(int L) {
     return (int)align_up((size_t)L, 32);
 }
 
-Layout make_layout(int njobs, int max_m, int max_n) {
+Layout make_layout(int njobs, int max_m, int max_n, bool pieces = false) {
     Layout lo;
     const int L = max(max_m, max_n), C = min(max_m, max_n);
     lo.lslot = slot_rows(max(L, 1));
@@ -1397,6 +1397,9 @@ Layout make_layout(int njobs, int max_m, int max_n) {
     lo.qstride = lo.nbmax * (lo.nbmax / 2);
     lo.off_vst = o; o = align_up(o + nj * lo.nbmax * sizeof(int), 256);
     lo.off_qst = o; o = align_up(o + nj * lo.qstride * sizeof(int), 256);
+    // the mixed form's bf16 piece planes of X (3 per job)
+    lo.off_P = o;
+    if (pieces) o = align_up(o + nj * 3 * 2 * (size_t)lo.lslot * lo.cslot * sizeof(uint16_t), 256);
     lo.total = o;
     return lo;
 }
@@ -1415,6 +1418,12 @@ extern "C" size_t mps_2q_workspace_bytes(int njobs, int max_m, int max_n, int d)
     return make_layout(njobs, max_m, max_n).total;
 }
 
+extern "C" size_t mps_2q_workspace_bytes_mixed(int njobs, int max_m, int max_n, int d) {
+    (void)d;
+    if (njobs <= 0 || max_m <= 0 || max_n <= 0) return 0;
+    return make_layout(njobs, max_m, max_n, true).total;
+}
+
 extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njobs,
                                   int max_m, int max_n, int d, void* workspace,
                                   size_t workspace_bytes, mps_svd_params* params) {
@@ -1431,7 +1440,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (d < 1 || d > 64) return fail(MPS_ERR_ARG, "mps_apply_2q_batch: qudit dimension must be 1..64");
     if (max_m <= 0 || max_n <= 0)
         return fail(MPS_ERR_ARG, "mps_apply_2q_batch: max_m/max_n must be positive");
-    const Layout lo = make_layout(njobs, max_m, max_n);
+    const bool mixed_req = params && params->precision == MPS_PRECISION_MIXED;
+    const Layout lo = make_layout(njobs, max_m, max_n, mixed_req);
     if (lo.lslot > 1792)
         return fail(MPS_ERR_ARG, "mps_apply_2q_batch: merged matrix longer than 1792 rows "
                                  "is beyond this build's shared-memory Jacobi kernel");
@@ -1462,6 +1472,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     g.qstamp = reinterpret_cast<int*>(ws + lo.off_qst);
     g.nbmax = lo.nbmax;
     g.qstride = lo.qstride;
+    g.P = mixed_req ? reinterpret_cast<uint16_t*>(ws + lo.off_P) : nullptr;
+    g.pplane = (size_t)2 * lo.lslot * lo.cslot;
 
     int max_sweeps = 40;
     float tol = 0.f;
@@ -1538,17 +1550,25 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
             MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
             if (mixed) {
-                // tensor-core block sweeps: no visit-skipping stamps and no
-                // round-dependency waits (sync.error stays 0)
-                if (sweeps == 1) MPS_CUDA_CHECK(cudaMemsetAsync(sync.error, 0, sizeof(int), s));
-                TwoQGeom gm = g;
-                gm.vstamp = nullptr;
-                gm.qstamp = nullptr;
+                // tensor-core block sweeps, one persistent launch per sweep
+                // with the same round flags and visit stamps as the SIMT
+                // form; X is split into its bf16 pieces once, before the
+                // first sweep (an expired wait stays in sync.error until the
+                // call returns)
+                if (sweeps == 1) {
+                    MPS_CUDA_CHECK(cudaMemsetAsync(sync.error, 0, sizeof(int), s));
+                    if (int e = tc_split_launch(njobs, g, s)) return e;
+                }
                 if (cmax > 2 * bc) {
-                    presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, gm, npow2, bc, 0);
+                    presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc,
+                                                                       sweeps * (rounds + 1));
                     MPS_LAUNCH_CHECK("presort_kernel");
                 }
-                rc = tc_sweep_launch(jobs, njobs, rounds, pairs, gm, tol2, s);
+                MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, sizeof(int), s));
+                MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
+                                               (size_t)njobs * lo.nbmax * sizeof(int), s));
+                rc = tc_sweep_launch(jobs, njobs, rounds, pairs, g, tol2, sync,
+                                     sweeps * (rounds + 1), s);
                 if (rc) return rc;
             } else {
                 if (cmax > 2 * bc) {
@@ -1594,6 +1614,11 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
             }
         }
         if (sweeps > max_sweeps) sweeps = max_sweeps;
+        if (mixed) {
+            // the tensor-core sweeps kept the columns in the piece planes
+            rc = tc_merge_launch(njobs, g, s);
+            if (rc) return rc;
+        }
     } else {
         converged = true;
         // single-column (or empty) jobs: nothing to rotate
@@ -1700,7 +1725,7 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     if (d < 1 || d > 64) return fail(MPS_ERR_ARG, "mps_apply_2q_batch_noalloc: qudit dimension must be 1..64");
     if (max_m <= 0 || max_n <= 0)
         return fail(MPS_ERR_ARG, "mps_apply_2q_batch_noalloc: max_m/max_n must be positive");
-    const Layout lo = make_layout(njobs, max_m, max_n);
+    const Layout lo = make_layout(njobs, max_m, max_n, false);
     if (lo.lslot > 1792)
         return fail(MPS_ERR_ARG, "mps_apply_2q_batch_noalloc: merged matrix longer than 1792 rows "
                                  "is beyond this build's shared-memory Jacobi kernel");
@@ -1737,6 +1762,8 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     g.qstamp = nullptr;
     g.nbmax = lo.nbmax;
     g.qstride = lo.qstride;
+    g.P = nullptr;
+    g.pplane = 0;
 
     int max_sweeps = 40;
     float tol = 0.f;

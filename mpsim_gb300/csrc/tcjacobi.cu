@@ -7,51 +7,70 @@
 // U = X/S from the final columns and whose right factor is formed afterwards
 // as U^H theta.
 //
-// The C columns of X (the L factor of theta, or theta) are split into blocks
-// of 32.  A sweep visits every pair of blocks once (circle-method rounds over
-// the norm-sorted column order, as in the SIMT form).  One visit of blocks
-// (I, J), Y = [X_I X_J] (L x 64 complex), by one 256-thread CTA:
+// Storage.  For the sweeps, X (FP32, the L factor of theta or theta) is held
+// as three bf16 piece planes P0, P1, P2 per job, laid out like X, with
+// x = p0 + p1 + p2 exactly (p0 = bf16(x), p1 = bf16(x - p0), p2 =
+// bf16(x - p0 - p1); both subtractions are exact, and the last residual has
+// at most 8 significant bits, so it is p2 itself, barring underflow).
+// tc_split_kernel writes the planes before the first sweep and tc_merge_kernel
+// sums them back into X after the last one; in between the visits read and
+// write pieces only (12 bytes a complex element instead of 8 + 12, and the
+// planes of a 32-job chi=256 call, 96 MB, mostly stay in L2).
+//
+// The C columns are split into blocks of 32.  A sweep visits every pair of
+// blocks once (circle-method rounds over the norm-sorted column order, as in
+// the SIMT form).  One visit of blocks (I, J), Y = [X_I X_J] (L x 64 complex),
+// by one 256-thread CTA:
 //   1. Gram:     G = Y^H Y (64 x 64 complex) on the tensor cores.  Real form:
 //                rows 0..63 of the operand tile are the columns of Y as
 //                interleaved (re, im) vectors of length 2L, rows 64..127 are
 //                T = -i Y; D[m, q] = sum over the 2L reals of tile row m times
-//                tile row q gives Re G (m < 64) and -Im G (m >= 64).
-//                K-major operands, K = 2L in chunks of 64 reals.
-//   2. Rotations on G in shared memory: two-sided Jacobi, 32 disjoint pairs
-//                per step (the 32 x 32 inter-block pairs in 32 steps, or all
-//                2016 pairs in 63 steps on a block's first visit of a
-//                sweep), accumulating the 64 x 64 unitary Q.  The convergence
-//                test runs first, in FP64 on the fresh Gram: a visit none of
-//                whose pairs has |G_pq|^2 > tol^2 G_pp G_qq changes nothing and
-//                skips steps 2 and 3.  The per-step rotation test and the
-//                rotation parameters are the FP32 ones of rot.cuh.
-//   3. Rotation: Y <- Y + Y E with E = Q - I, skipped when the visit rotated
-//                nothing.  The tensor cores form D = Y E; the epilogue adds
-//                Y + D in FP32 with round-to-nearest.  Real form:
-//                D[(r, c), q] = sum_p Y[(r, c), p] Re E_pq + T[(r, c), p]
-//                (-Im E_pq): the SAME shared-memory tile as step 1, now read
-//                as an MN-major A operand (M = the 2L reals, 64 per swizzle
-//                row; K = the 128 tile rows), times a K-major B operand holding
-//                (Re E, -Im E).  M = 128 reals per MMA.
-// Why the update form: the tensor core's FP32 accumulation truncates toward
-// zero (it does not round to nearest), so a product accumulated over many
-// MMAs comes out slightly small.  Y Q re-accumulates all of Y in every visit
-// and shrank every singular value by ~5e-5 over a chi=256 SVD; D = Y E is
-// small once the rotations are (after the first sweeps), and its bias goes
-// with it.  The piece products are also issued smallest first, so the
-// accumulator is small for all but the last eight MMAs.
-// Every FP32 value is split into three bf16 pieces and each product sums
-// the six piece products of order <= 2 (tc.cuh): FP32-grade Gram entries
-// and rotations, with the tensor pipe doing the O(L) work that the SIMT form
-// does with FMAs.  The new squared column norms (the diagonal of Q^H G Q) go
-// to cnrm for the next sweep's sort.
+//                tile row q gives Re G (m < 64) and -Im G (m >= 64).  T's
+//                pieces are Y's with each packed (re, im) pair turned into
+//                (im, -re): a half-word swap and a sign flip.  K-major
+//                operands, K = 2L in chunks of 64 reals (the six piece
+//                products of order <= 2 per K step), two tile buffers so that
+//                the stores of chunk c + 1 overlap the MMAs of chunk c.  Each
+//                chunk accumulates into its own TMEM buffer and the chunks are
+//                summed in FP32 registers with round-to-nearest: tcgen05's
+//                FP32 accumulation truncates toward zero, and one accumulator
+//                over all 2L reals left Gram errors of ~1e-6 |y_p||y_q|, the
+//                size of the convergence tolerance, which cost sweeps.
+//   2. Convergence test and rotations on G.  The off-diagonal test runs
+//                first, in FP64 on the fresh Gram: a visit none of whose
+//                pairs has |G_pq|^2 > tol^2 G_pp G_qq changes nothing and
+//                skips the rest.  Otherwise two-sided Jacobi on G in shared
+//                memory, 32 disjoint pairs per step (the 32 x 32 inter-block
+//                pairs in 32 steps, or all 2016 pairs in 63 steps on a block's
+//                first visit of a sweep), accumulating E = Q - I.  Every warp
+//                computes the 32 rotations of a step (lane k: pair k, the FP32
+//                parameters of rot.cuh), so a step where no pair rotates is
+//                skipped by all warps alike, without a barrier.  G' = R^H G R
+//                in two passes with the same thread layout (lane k: pair k's
+//                two columns, warp w: rows w, w + 8, ...): H = G R written
+//                conjugate-transposed, then G' = H^H R (G is Hermitian); E
+//                takes R in the second pass.
+//   3. Update:   Y <- Y + Y E, skipped when the visit rotated nothing.  The
+//                tensor cores form D = Y E from piece tiles of Y read as an
+//                MN-major A operand (M = 128 reals of the column, K = the 128
+//                tile rows) times a K-major B holding (Re E, -Im E); the
+//                epilogue adds D to Y (summed from its pieces) in FP32 with
+//                round-to-nearest and writes the new pieces.  The update form
+//                keeps the truncation small: D = Y E is small once the
+//                rotations are (accumulating Y Q in full shrank every singular
+//                value by ~5e-5 over a chi=256 SVD).  The piece products are
+//                issued smallest first.
+// The new squared column norms (the diagonal of Q^H G Q) go to cnrm for the
+// next sweep's sort.
 //
-// Shared memory (about 82 KB, two CTAs per SM):
-//   R0 [0, 48K):   step 1: three 16 KB bf16 piece tiles (128 rows x 128 B);
-//                  step 2: G (64 x 65 complex, padded rows);
-//                  step 3: the three B-operand pieces of Q (16 KB each).
-//   R1 [48K, 80K): step 2: E = Q - I (64 x 64 complex);
-//                  step 3: one A piece tile (2 x 16 KB M-groups).
+// Shared memory (96 KB + the small arrays: two CTAs per SM):
+//   [0, 96K)   step 1: two tile buffers, each three 16 KB piece tiles
+//              (128 rows x 128 B, 128-byte swizzle)
+//   [0, 32K)   step 2: G (64 x 64 complex, columns XOR-swizzled by the row)
+//   [32K, 64K) step 2: H^H, the first pass's output (same layout)
+//   [64K, 96K) step 2: E = Q - I (64 x 64 complex, row-major)
+//   [0, 48K)   step 3: the three B-operand pieces of E (16 KB each)
+//   [48K, 80K) step 3: one A piece tile (two 16 KB M-groups)
 #include "rot.cuh"
 #include "tc.cuh"
 #include "twoq.cuh"
@@ -63,73 +82,40 @@ constexpr int TJ_T = 256;                  // threads per CTA
 constexpr int TJ_BC = 32;                  // columns per block
 constexpr int TJ_W = 2 * TJ_BC;            // columns per visit
 constexpr uint32_t TJ_PIECE = 16384;       // 128 rows x 128 B
-constexpr uint32_t TJ_R1 = 3 * TJ_PIECE;   // 48 KB
-constexpr uint32_t TJ_AUX = TJ_R1 + 2 * TJ_PIECE;   // 80 KB: small arrays
-constexpr int TJ_GS = TJ_W + 1;            // padded row stride of G (complex): column reads
-constexpr int TJ_QS = TJ_W;                // row stride of Q (its accesses are row-contiguous)
-constexpr uint32_t TJ_TMEM_COLS = 64;
+constexpr uint32_t TJ_GTILE = 3 * TJ_PIECE;         // one Gram tile buffer (48 KB)
+constexpr uint32_t TJ_GBUF = TJ_W * TJ_W * 8;       // one 64 x 64 complex buffer (32 KB)
+constexpr uint32_t TJ_HOFF = TJ_GBUF;               // H^H at 32 KB
+constexpr uint32_t TJ_EOFF = 2 * TJ_GBUF;           // E at 64 KB
+constexpr uint32_t TJ_AOFF = 3 * TJ_PIECE;          // the update's A tile at 48 KB
+constexpr uint32_t TJ_AUX = 2 * TJ_GTILE;           // 96 KB: small arrays
+constexpr uint32_t TJ_TMEM_COLS = 128;              // two 64-column Gram accumulators
 constexpr int TJ_WAIT_LIMIT = 1 << 14;
+static_assert(TJ_EOFF + TJ_GBUF <= TJ_AUX, "E overlaps the small arrays");
+static_assert(TJ_AOFF + 2 * TJ_PIECE <= TJ_AUX, "the update's A tile overlaps the small arrays");
 
 // Cycles spent in the three steps of a visit, summed over the CTAs of every
 // visit since the last reset: [0] Gram, [1] rotations on G, [2] Y <- Y + Y E,
-// [3] visits.  Read with mps_tc_profile.
-__device__ unsigned long long g_tj_cycles[4];
+// [3] visits, [4] visits that rotated, [5] inner steps that rotated, [6]
+// pairs rotated, [7] cycles spent waiting for the blocks' previous round,
+// [8] CTA lifetimes of the sweep kernel, [9] its CTAs.  Read with
+// mps_tc_profile.
+__device__ unsigned long long g_tj_cycles[10];
 
 struct Aux {
-    uint64_t bar;
+    uint64_t bar[2];      // MMA completion, one per Gram tile buffer
     uint32_t tmem;
-    int rotated;          // any pair of this visit rotated
+    int item, abort, skip;   // the claimed visit, the stop flag, its skip decision
+    int rotated;          // some pair of this visit needs a rotation
     int col[TJ_W];        // physical column of each visit column (-1: zero padding)
-    float tp[TJ_W / 2];   // rotation parameters of the current step
-    cf sigma[TJ_W / 2];
-    int pp[TJ_W / 2], pq[TJ_W / 2];
-    float cmax;           // largest squared cosine of a rotated pair
+    float diag[TJ_W];     // diagonal of G (squared column norms)
+    float cmax;           // largest squared cosine of the visit's pairs
 };
 constexpr size_t TJ_SMEM = TJ_AUX + sizeof(Aux) + 1024;
 
-// Two FP32 values -> piece `which` of each, packed as one 32-bit word.
-__device__ __forceinline__ uint32_t pack_piece(float a, float b, int which) {
-    const tc::Split3 sa = tc::split3(a), sb = tc::split3(b);
-    const __nv_bfloat16 xa = which == 0 ? sa.p0 : (which == 1 ? sa.p1 : sa.p2);
-    const __nv_bfloat16 xb = which == 0 ? sb.p0 : (which == 1 ? sb.p1 : sb.p2);
-    return (uint32_t)__bfloat16_as_ushort(xa) | ((uint32_t)__bfloat16_as_ushort(xb) << 16);
-}
-
-// 8 reals -> the 16-byte chunk of piece `which` at off (registers only: a
-// runtime-indexed local array would live in local memory).
-__device__ __forceinline__ void put_piece(uint8_t* base, uint32_t off, const float* v, int which) {
-    uint4 w;
-    w.x = pack_piece(v[0], v[1], which);
-    w.y = pack_piece(v[2], v[3], which);
-    w.z = pack_piece(v[4], v[5], which);
-    w.w = pack_piece(v[6], v[7], which);
-    *reinterpret_cast<uint4*>(base + off) = w;
-}
-
-// 8 reals -> the 16-byte chunks of all three pieces, in tiles `stride` apart.
-__device__ __forceinline__ void put_pieces(uint8_t* base, uint32_t stride, uint32_t off,
-                                           const float* v) {
-    uint32_t w[3][4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        const tc::Split3 a = tc::split3(v[2 * e]), b = tc::split3(v[2 * e + 1]);
-        w[0][e] = (uint32_t)__bfloat16_as_ushort(a.p0) | ((uint32_t)__bfloat16_as_ushort(b.p0) << 16);
-        w[1][e] = (uint32_t)__bfloat16_as_ushort(a.p1) | ((uint32_t)__bfloat16_as_ushort(b.p1) << 16);
-        w[2][e] = (uint32_t)__bfloat16_as_ushort(a.p2) | ((uint32_t)__bfloat16_as_ushort(b.p2) << 16);
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        *reinterpret_cast<uint4*>(base + i * stride + off) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
-}
-
-// T = -i Y: (re, im) -> (im, -re).
-__device__ __forceinline__ void twist8(const float* v, float* t) {
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        t[2 * e] = v[2 * e + 1];
-        t[2 * e + 1] = -v[2 * e];
-    }
-}
+// Element (r, c) of a 64 x 64 complex buffer; the column is XOR-swizzled by
+// the row, so that lanes reading or writing one column of different rows
+// (the transposed writes of the first pass) spread over the banks.
+__device__ __forceinline__ int gidx(int r, int c) { return r * TJ_W + (c ^ (r & 31)); }
 
 __device__ __forceinline__ bool wait_mma(uint64_t* bar, unsigned& phase) {
     const bool ok = tc::mbar_wait_bounded(bar, phase, TJ_WAIT_LIMIT);
@@ -148,185 +134,231 @@ __device__ __forceinline__ void inner_pair(bool full, int s, int k, int& p, int&
     }
 }
 
-// Phase-1 loads of rows 32c..32c+31: task (p, grp) = 8 reals of column p.
-__device__ __forceinline__ void load_gram_chunk(float (&pre)[2][8], const float* X, const int* col,
-                                                int lslot, int c, int tid) {
+// Columns x (p) and y (q) of a row times R = [[1 - tp, conj(s)], [-s, 1 - tp]]
+// in the tau form of rot.cuh (an explicit c = 1 - tp would round to 1 for
+// small angles and inflate the norms).
+__device__ __forceinline__ void rotate_cols(cf& x, cf& y, float tp, cf sg) {
+    const cf nx = csub(x, cadd(cscale(x, tp), cmul(y, sg)));
+    const cf ny = cadd(y, csub(cmul(x, cconj(sg)), cscale(y, tp)));
+    x = nx;
+    y = ny;
+}
+
+// T = -i Y on 8 packed bf16 (four (re, im) pairs, re in the low half of each
+// word): (re, im) -> (im, -re).  Exact: the split is odd-symmetric.
+__device__ __forceinline__ uint4 twist_packed(uint4 w) {
+    const uint32_t sign = 0x80000000u;
+    w.x = __byte_perm(w.x, 0, 0x1032) ^ sign;
+    w.y = __byte_perm(w.y, 0, 0x1032) ^ sign;
+    w.z = __byte_perm(w.z, 0, 0x1032) ^ sign;
+    w.w = __byte_perm(w.w, 0, 0x1032) ^ sign;
+    return w;
+}
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
+    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+// 8 reals -> the 16-byte chunks of all three pieces, in buffers `stride`
+// bytes apart.
+__device__ __forceinline__ void put_pieces(uint8_t* base, size_t stride, uint32_t off,
+                                           const float* v) {
+    uint32_t w[3][4];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int task = tid + TJ_T * h;
-        const int p = task >> 3, grp = task & 7;
+    for (int e = 0; e < 4; ++e) {
+        const tc::Split3 a = tc::split3(v[2 * e]), b = tc::split3(v[2 * e + 1]);
+        w[0][e] = pack2(a.p0, b.p0);
+        w[1][e] = pack2(a.p1, b.p1);
+        w[2][e] = pack2(a.p2, b.p2);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        *reinterpret_cast<uint4*>(base + i * stride + off) =
+            make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+}
+
+__device__ __forceinline__ float bf16_bits(uint16_t u) {
+    return __uint_as_float((uint32_t)u << 16);
+}
+
+// Gram task t (0..1535) = (column p, piece i, 16-byte chunk g of the 128
+// bytes a piece column holds for 32 rows).
+__device__ __forceinline__ void gram_task(int t, int& p, int& i, int& g) {
+    p = t / 24;
+    const int rem = t - 24 * p;
+    i = rem >> 3;
+    g = rem & 7;
+}
+
+// Step-1 loads of rows 32c..32c+31: 1536 tasks, 6 a thread.
+__device__ __forceinline__ void load_gram_pieces(uint4 (&v)[6], const uint16_t* P, size_t pplane,
+                                                 const int* col, int lslot, int c, int tid) {
+#pragma unroll
+    for (int h = 0; h < 6; ++h) {
+        int p, i, g;
+        gram_task(tid + TJ_T * h, p, i, g);
         const int cc = col[p];
         if (cc >= 0) {
-            const float4* src = reinterpret_cast<const float4*>(
-                X + ((size_t)cc * lslot + (size_t)c * 32) * 2 + grp * 8);
-            const float4 a = __ldcg(src), b = __ldcg(src + 1);
-            pre[h][0] = a.x; pre[h][1] = a.y; pre[h][2] = a.z; pre[h][3] = a.w;
-            pre[h][4] = b.x; pre[h][5] = b.y; pre[h][6] = b.z; pre[h][7] = b.w;
+            const uint16_t* src = P + i * pplane + (size_t)cc * 2 * lslot + (size_t)c * 64 + g * 8;
+            v[h] = __ldcg(reinterpret_cast<const uint4*>(src));
         } else {
-#pragma unroll
-            for (int e = 0; e < 8; ++e) pre[h][e] = 0.f;
+            v[h] = make_uint4(0u, 0u, 0u, 0u);
         }
     }
 }
 
-// Phase-3 loads of rows 64cp..64cp+63: task (p, grp) = 8 reals of column p.
-__device__ __forceinline__ void load_rot_chunk(float (&y)[4][8], const float* X, const int* col,
-                                               int lslot, int cp, int tid) {
+// Step-3 loads of piece `ia` of rows 64cp..64cp+63 (128 reals, 256 bytes a
+// column): task t (0..1023) = (column p, 16-byte chunk g), 4 a thread.
+__device__ __forceinline__ void load_rot_piece(uint4 (&v)[4], const uint16_t* P, size_t pplane,
+                                               const int* col, int lslot, int cp, int ia, int tid) {
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
-        const int task = tid + TJ_T * h;
-        const int p = task >> 4, grp = task & 15;
+        const int t = tid + TJ_T * h;
+        const int p = t >> 4, g = t & 15;
         const int cc = col[p];
         if (cc >= 0) {
-            const float4* src = reinterpret_cast<const float4*>(
-                X + ((size_t)cc * lslot + (size_t)cp * 64) * 2 + grp * 8);
-            const float4 a = __ldcg(src), b = __ldcg(src + 1);
-            y[h][0] = a.x; y[h][1] = a.y; y[h][2] = a.z; y[h][3] = a.w;
-            y[h][4] = b.x; y[h][5] = b.y; y[h][6] = b.z; y[h][7] = b.w;
+            const uint16_t* src = P + ia * pplane + (size_t)cc * 2 * lslot + (size_t)cp * 128 + g * 8;
+            v[h] = __ldcg(reinterpret_cast<const uint4*>(src));
         } else {
-#pragma unroll
-            for (int e = 0; e < 8; ++e) y[h][e] = 0.f;
+            v[h] = make_uint4(0u, 0u, 0u, 0u);
         }
     }
 }
 
-__global__ void __launch_bounds__(TJ_T, 2)
-tc_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, double tol2d,
-                float tol2) {
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                               ~uintptr_t(1023));
-    Aux& ax = *reinterpret_cast<Aux*>(smem + TJ_AUX);
-    uint8_t* R0 = smem;
-    uint8_t* R1 = smem + TJ_R1;
-    cf* G = reinterpret_cast<cf*>(R0);
-    cf* Q = reinterpret_cast<cf*>(R1);
+// Adds the 32 TMEM columns at taddr (this thread's lane) into acc.
+__device__ __forceinline__ void tmem_accumulate(uint32_t taddr, float (&acc)[32]) {
+    float v[32];
+    tc::tmem_ld32(taddr, v);
+#pragma unroll
+    for (int e = 0; e < 32; ++e) acc[e] += v[e];
+}
 
-    const int j = blockIdx.y;
-    if (__ldg(g.done + j)) return;
-    const mps_2q_job job = jobs[j];
-    const int m = job.chi_l * g.d, n = job.chi_r * g.d;
-    const int C = min(m, n);
-    if (job_tracks_v(m, n, job.keep_left_canonical) || C < TJ_W) {
-        // only left-canonical tall jobs of 64+ columns take these sweeps
-        if (threadIdx.x == 0 && blockIdx.x == 0 && round == 0) atomicExch(g.counter + 2, 1);
-        return;
-    }
-    int nb = (C + TJ_BC - 1) / TJ_BC;
-    if (nb < 2) nb = 2;
-    nb += nb & 1;
-    if (round >= nb - 1 || (int)blockIdx.x >= nb / 2) return;
-    int I, J;
-    tournament_pair(nb, round, blockIdx.x, I, J);
-    const bool full = round == 0;
-
+// One visit of blocks (I, J) of job j (see the file comment).  All threads
+// call it; returns whether it rotated anything and clears ok when a bounded
+// MMA wait expired (the outputs are then invalid).
+__device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bool full,
+                                      double tol2d, float tol2, uint8_t* smem, Aux& ax,
+                                      uint32_t tmem, unsigned& ph0, unsigned& ph1, bool& ok) {
+    cf* const G = reinterpret_cast<cf*>(smem);
+    cf* const H = reinterpret_cast<cf*>(smem + TJ_HOFF);
+    cf* const E = reinterpret_cast<cf*>(smem + TJ_EOFF);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int lslot = g.lslot;
-    float* X = reinterpret_cast<float*>(g.X + (size_t)j * lslot * g.cslot);
+    const size_t pplane = g.pplane;
+    uint16_t* P = g.P + (size_t)j * 3 * pplane;
+    // this thread's TMEM lane quarter and its 32 accumulator columns
+    const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32u * (uint32_t)(warp >> 2);
 
     if (tid < TJ_W) {
         const int pos = (tid < TJ_BC ? I * TJ_BC : J * TJ_BC - TJ_BC) + tid;
         ax.col[tid] = pos < g.cslot ? __ldcg(g.cmap + (size_t)j * g.cslot + pos) : -1;
     }
     if (tid == 0) {
-        mbar_init(&ax.bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         ax.rotated = 0;
         ax.cmax = 0.f;
     }
-    if (warp == 0) {
-        tc::tmem_alloc(&ax.tmem, TJ_TMEM_COLS);
-        tc::tmem_relinquish();
-    }
-    tc::fence_before_sync();
     __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tmem = ax.tmem;
-    unsigned phase = 0;
-    bool ok = true;
-
     const long long c0 = clock64();
-    // ---- 1. Gram -------------------------------------------------------
-    // chunk c: rows 32c..32c+31 (64 reals); task (p, grp): 8 reals of column p
-    const int nchunk = lslot / 32;
-    float pre[2][8];
-    constexpr uint32_t IDESC_G = tc::idesc_bf16(128, 64, false, false);
-    load_gram_chunk(pre, X, ax.col, lslot, 0, tid);
-    for (int c = 0; c < nchunk; ++c) {
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int task = tid + TJ_T * h;
-            const int p = task >> 3, grp = task & 7;
-            float t[8];
-            twist8(pre[h], t);
-            put_pieces(R0, TJ_PIECE, tc::sw128_off(p, grp * 8), pre[h]);
-            put_pieces(R0, TJ_PIECE, tc::sw128_off(TJ_W + p, grp * 8), t);
-        }
-        tc::fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            tc::fence_after_sync();
-            const uint32_t s0 = tc::smem_u32(R0);
-            const int pa[6] = {2, 1, 0, 1, 0, 0};
-            const int pb[6] = {0, 1, 2, 0, 1, 0};
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks)
-#pragma unroll
-                for (int q = 0; q < 6; ++q)
-                    tc::mma_bf16(tmem, tc::sdesc(s0 + pa[q] * TJ_PIECE + ks * 32, 16, 1024),
-                                 tc::sdesc(s0 + pb[q] * TJ_PIECE + ks * 32, 16, 1024), IDESC_G,
-                                 (c | ks | q) != 0);
-            tc::mma_commit(&ax.bar);
-        }
-        if (c + 1 < nchunk) load_gram_chunk(pre, X, ax.col, lslot, c + 1, tid);  // overlaps the MMAs
-        ok = __syncthreads_and(wait_mma(&ax.bar, phase)) != 0;
-        if (!ok) break;
-    }
-    tc::fence_after_sync();
 
-    // ---- TMEM -> G (R0), E = Q - I = 0 (R1) --------------------------------
-    if (ok) {
-        const int mrow = 32 * (warp & 3) + lane;           // tile row of this lane
+    // ---- 1. Gram -------------------------------------------------------
+    {
+        const int nchunk = lslot / 32;
+        constexpr uint32_t IDESC_G = tc::idesc_bf16(128, 64, false, false);
+        float acc[32];
+#pragma unroll
+        for (int e = 0; e < 32; ++e) acc[e] = 0.f;
+        uint4 pre[6];
+        load_gram_pieces(pre, P, pplane, ax.col, lslot, 0, tid);
+        int waited = -1;                  // chunks <= waited are summed into acc
+        for (int c = 0; c < nchunk; ++c) {
+            const int b = c & 1;
+            if (c >= 2) {
+                // tile buffer b and accumulator b were used by chunk c - 2
+                ok = __syncthreads_and(b ? wait_mma(&ax.bar[1], ph1) : wait_mma(&ax.bar[0], ph0)) != 0;
+                if (!ok) break;
+                tc::fence_after_sync();
+                tmem_accumulate(tlane + 64u * b, acc);
+                tc::fence_before_sync();
+                waited = c - 2;
+            }
+            uint8_t* tile = smem + b * TJ_GTILE;
+#pragma unroll
+            for (int h = 0; h < 6; ++h) {
+                int p, i, gg;
+                gram_task(tid + TJ_T * h, p, i, gg);
+                uint8_t* t = tile + i * TJ_PIECE;
+                *reinterpret_cast<uint4*>(t + tc::sw128_off(p, gg * 8)) = pre[h];
+                *reinterpret_cast<uint4*>(t + tc::sw128_off(TJ_W + p, gg * 8)) = twist_packed(pre[h]);
+            }
+            tc::fence_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint32_t s0 = tc::smem_u32(tile);
+                // piece products smallest first: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)
+                const int pa[6] = {2, 1, 0, 1, 0, 0};
+                const int pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+                for (int ks = 0; ks < 4; ++ks)
+#pragma unroll
+                    for (int q = 0; q < 6; ++q)
+                        tc::mma_bf16(tmem + 64u * b,
+                                     tc::sdesc(s0 + pa[q] * TJ_PIECE + ks * 32, 16, 1024),
+                                     tc::sdesc(s0 + pb[q] * TJ_PIECE + ks * 32, 16, 1024), IDESC_G,
+                                     (ks | q) != 0);
+                tc::mma_commit(&ax.bar[b]);
+            }
+            if (c + 1 < nchunk) load_gram_pieces(pre, P, pplane, ax.col, lslot, c + 1, tid);
+        }
+        // the last one or two chunks (every phase is waited on, so the
+        // barriers' parities stay in step)
+        for (int c = waited + 1; ok && c < nchunk; ++c) {
+            const int b = c & 1;
+            ok = __syncthreads_and(b ? wait_mma(&ax.bar[1], ph1) : wait_mma(&ax.bar[0], ph0)) != 0;
+            if (!ok) break;
+            tc::fence_after_sync();
+            tmem_accumulate(tlane + 64u * b, acc);
+        }
+        if (!ok) return false;
+        // acc -> G: D rows 0..63 are Re G, rows 64..127 are -Im G
+        tc::fence_before_sync();
+        __syncthreads();                                   // the tile buffers are dead
+        const int mrow = 32 * (warp & 3) + lane;
         const int q0 = 32 * (warp >> 2);
-        float v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + q0, v);
-        __syncthreads();                                   // R0 pieces are dead
         if (mrow < TJ_W) {
 #pragma unroll
-            for (int e = 0; e < 32; ++e) G[mrow * TJ_GS + q0 + e].x = v[e];
+            for (int e = 0; e < 32; ++e) G[gidx(mrow, q0 + e)].x = acc[e];
         } else {
 #pragma unroll
-            for (int e = 0; e < 32; ++e) G[(mrow - TJ_W) * TJ_GS + q0 + e].y = -v[e];
+            for (int e = 0; e < 32; ++e) G[gidx(mrow - TJ_W, q0 + e)].y = -acc[e];
         }
-        for (int e = tid; e < TJ_W * TJ_W; e += TJ_T) {
-            const int r = e / TJ_W, c = e % TJ_W;
-            Q[r * TJ_QS + c] = cmake(0.f, 0.f);
-        }
-        __syncthreads();
-        if (tid < TJ_W) G[tid * TJ_GS + tid].y = 0.f;
-        __syncthreads();
     }
-
+    for (int e = tid; e < TJ_W * TJ_W; e += TJ_T) E[e] = cmake(0.f, 0.f);
+    __syncthreads();
+    if (tid < TJ_W) {
+        G[gidx(tid, tid)].y = 0.f;
+        ax.diag[tid] = G[gidx(tid, tid)].x;
+    }
+    __syncthreads();
     const long long c1 = clock64();
-    // ---- 2. rotations on G -------------------------------------------------
-    // The off-diagonal convergence test, in FP64 on the fresh Gram: the
-    // visit's pairs (the 32 x 32 inter-block pairs, or all 2016 on a full
-    // visit) with |G_pq|^2 > tol^2 G_pp G_qq.  None: the visit changes nothing
-    // and steps 2 and 3 are skipped.  The largest squared cosine goes to the
-    // job's convergence record.
-    if (ok) {
+
+    // ---- 2. convergence test (FP64) and rotations on G ----------------------
+    // The visit's pairs (the 32 x 32 inter-block pairs, or all 2016 on a full
+    // visit) with |G_pq|^2 > tol^2 G_pp G_qq; the largest squared cosine goes
+    // to the job's convergence record.
+    {
         float cmax = 0.f;
         int any = 0;
         for (int e = tid; e < TJ_W * TJ_W; e += TJ_T) {
             const int p = e / TJ_W, q = e % TJ_W;
             if (q <= p || (!full && (p >= TJ_BC || q < TJ_BC))) continue;
-            const float a = G[p * TJ_GS + p].x, b = G[q * TJ_GS + q].x;
-            const cf gam = G[p * TJ_GS + q];
+            const float a = ax.diag[p], b = ax.diag[q];
+            const cf gam = G[gidx(p, q)];
             const double g2 = (double)gam.x * gam.x + (double)gam.y * gam.y;
             const double ab = (double)a * (double)b;
             if (a > 0.f && b > 0.f && g2 > tol2d * ab) {
                 any = 1;
-                cmax = fmaxf(cmax, (float)(g2 / ab));
+                cmax = fmaxf(cmax, (float)g2 / (float)ab);
             }
         }
         cmax = warp_max(cmax);
@@ -337,101 +369,92 @@ tc_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, doub
         }
         __syncthreads();
     }
-    const bool work = ok && ax.rotated;
+    const bool work = ax.rotated != 0;
     const int nsteps = full ? TJ_W - 1 : TJ_BC;
+    int rsteps = 0, rpairs = 0;
     for (int s = 0; work && s < nsteps; ++s) {
-        if (warp == 0) {
-            int p, q;
-            inner_pair(full, s, lane, p, q);
-            const float a = G[p * TJ_GS + p].x, b = G[q * TJ_GS + q].x;
-            const cf gam = G[p * TJ_GS + q];
+        // this warp's copy of the step's 32 rotations: lane k holds pair k
+        int p, q;
+        inner_pair(full, s, lane, p, q);
+        float tp = 0.f;
+        cf sg = cmake(0.f, 0.f);
+        bool rot;
+        {
+            const float a = ax.diag[p], b = ax.diag[q];
+            const cf gam = G[gidx(p, q)];
             // per-step rotation decision in FP32 (the SIMT form's test)
-            const bool rot = pair_cos2(gam, cabs2(gam), a, b) > tol2;
-            float tp = 0.f;
-            cf sg = cmake(0.f, 0.f);
+            rot = pair_cos2(gam, cabs2(gam), a, b) > tol2;
             if (rot) {
                 const Rot r = make_rot(a, b, gam);
                 tp = r.tp;
                 sg = r.sigma;
             }
-            ax.tp[lane] = tp;
-            ax.sigma[lane] = sg;
-            ax.pp[lane] = p;
-            ax.pq[lane] = q;
+        }
+        // every warp holds the same 32 decisions: a step without a rotation
+        // is skipped by all of them
+        const unsigned rmask = __ballot_sync(0xffffffffu, rot);
+        if (!rmask) continue;
+        ++rsteps;
+        rpairs += __popc(rmask);
+        // pass 1: H = G R, stored as H^H
+#pragma unroll 4
+        for (int h = 0; h < TJ_W / 8; ++h) {
+            const int r = warp + 8 * h;
+            cf x = G[gidx(r, p)], y = G[gidx(r, q)];
+            if (rot) rotate_cols(x, y, tp, sg);
+            H[gidx(p, r)] = cconj(x);
+            H[gidx(q, r)] = cconj(y);
         }
         __syncthreads();
-        // G <- R^H G R on the 2x2 blocks (pair a, pair b): 1024 blocks, 4 each
-#pragma unroll 1
-        for (int h = 0; h < 4; ++h) {
-            const int a = tid >> 3, b = (tid & 7) * 4 + h;
-            const int pa = ax.pp[a], qa = ax.pq[a], pb = ax.pp[b], qb = ax.pq[b];
-            const float ta = ax.tp[a], tb = ax.tp[b];
-            const cf sa = ax.sigma[a], sb = ax.sigma[b];
-            if (ta == 0.f && tb == 0.f && sa.x == 0.f && sa.y == 0.f && sb.x == 0.f && sb.y == 0.f)
-                continue;
-            cf m00 = G[pa * TJ_GS + pb], m01 = G[pa * TJ_GS + qb];
-            cf m10 = G[qa * TJ_GS + pb], m11 = G[qa * TJ_GS + qb];
-            // Both sides in the implicit-c ("tau") form of rot.cuh, R = I + D
-            // with D = [[-tp, conj(s)], [-s, -tp]]: an explicit c = 1 - tp
-            // rounds to 1 for small angles and every such rotation would
-            // inflate the norms.  M <- M R_b, then M <- R_a^H M.
-            const cf n00 = csub(m00, cadd(cscale(m00, tb), cmul(m01, sb)));
-            const cf n01 = cadd(m01, csub(cmul(m00, cconj(sb)), cscale(m01, tb)));
-            const cf n10 = csub(m10, cadd(cscale(m10, tb), cmul(m11, sb)));
-            const cf n11 = cadd(m11, csub(cmul(m10, cconj(sb)), cscale(m11, tb)));
-            m00 = csub(n00, cadd(cscale(n00, ta), cmul(cconj(sa), n10)));
-            m01 = csub(n01, cadd(cscale(n01, ta), cmul(cconj(sa), n11)));
-            m10 = cadd(n10, csub(cmul(sa, n00), cscale(n10, ta)));
-            m11 = cadd(n11, csub(cmul(sa, n01), cscale(n11, ta)));
-            if (a == b) {                 // the rotated pair's own block
-                m00.y = 0.f;
-                m11.y = 0.f;
-                if (ta != 0.f || sa.x != 0.f || sa.y != 0.f) {
-                    m01 = cmake(0.f, 0.f);
-                    m10 = cmake(0.f, 0.f);
-                }
-            }
-            G[pa * TJ_GS + pb] = m00;
-            G[pa * TJ_GS + qb] = m01;
-            G[qa * TJ_GS + pb] = m10;
-            G[qa * TJ_GS + qb] = m11;
-        }
-        // Q <- Q R kept as E = Q - I: rows r, pair b (2048 tasks, 8 each)
+        // pass 2: G' = H^H R (= R^H G R), and E <- E R (E = Q - I: the
+        // identity is added back here only)
 #pragma unroll 2
-        for (int h = 0; h < 8; ++h) {
-            const int task = tid + TJ_T * h;
-            const int b = task & 31, r = task >> 5;
-            const float tb = ax.tp[b];
-            const cf sb = ax.sigma[b];
-            if (tb == 0.f && sb.x == 0.f && sb.y == 0.f) continue;
-            const int pb = ax.pp[b], qb = ax.pq[b];
-            const cf ex = Q[r * TJ_QS + pb], ey = Q[r * TJ_QS + qb];
-            // tau form, as for G, on Q's columns x = e_pb + E[:, pb],
-            // y = e_qb + E[:, qb]; the identity is added back here only
-            const cf x = cmake(ex.x + (r == pb ? 1.f : 0.f), ex.y);
-            const cf y = cmake(ey.x + (r == qb ? 1.f : 0.f), ey.y);
-            Q[r * TJ_QS + pb] = csub(ex, cadd(cscale(x, tb), cmul(y, sb)));
-            Q[r * TJ_QS + qb] = cadd(ey, csub(cmul(x, cconj(sb)), cscale(y, tb)));
+        for (int h = 0; h < TJ_W / 8; ++h) {
+            const int r = warp + 8 * h;
+            cf x = H[gidx(r, p)], y = H[gidx(r, q)];
+            if (rot) rotate_cols(x, y, tp, sg);
+            if (r == p) {                 // (p, p) and (p, q)
+                x.y = 0.f;
+                if (rot) y = cmake(0.f, 0.f);
+                ax.diag[p] = x.x;
+            } else if (r == q) {          // (q, p) and (q, q)
+                y.y = 0.f;
+                if (rot) x = cmake(0.f, 0.f);
+                ax.diag[q] = y.x;
+            }
+            G[gidx(r, p)] = x;
+            G[gidx(r, q)] = y;
+            if (rot) {
+                const cf ex = E[r * TJ_W + p], ey = E[r * TJ_W + q];
+                cf ux = cmake(ex.x + (r == p ? 1.f : 0.f), ex.y);
+                cf uy = cmake(ey.x + (r == q ? 1.f : 0.f), ey.y);
+                E[r * TJ_W + p] = csub(ex, cadd(cscale(ux, tp), cmul(uy, sg)));
+                E[r * TJ_W + q] = cadd(ey, csub(cmul(ux, cconj(sg)), cscale(uy, tp)));
+            }
         }
         __syncthreads();
     }
-
     const long long c2 = clock64();
-    // new squared norms for the next sweep's sort (a visit with nothing to
-    // rotate leaves them as they were), and this visit's largest cosine
-    if (work && tid < TJ_W) {
+    const bool rotated = work && rsteps > 0;
+
+    // new squared norms for the next sweep's sort, and this visit's largest
+    // cosine (a pair over the FP64 test that the FP32 step test does not
+    // rotate is on the tolerance's edge: it counts as converged, or the job
+    // would see the same Gram again every sweep)
+    if (rotated && tid < TJ_W) {
         const int col = ax.col[tid];
-        if (col >= 0) g.cnrm[(size_t)j * g.cslot + col] = G[tid * TJ_GS + tid].x;
+        if (col >= 0) g.cnrm[(size_t)j * g.cslot + col] = ax.diag[tid];
     }
-    if (ok && tid == 0 && ax.rotated)
-        atomicMax(reinterpret_cast<int*>(g.offmax + j), __float_as_int(ax.cmax));
+    if (rotated && tid == 0) atomicMax(reinterpret_cast<int*>(g.offmax + j), __float_as_int(ax.cmax));
 
     // ---- 3. Y <- Y + Y E ---------------------------------------------------
-    if (work) {
-        // B pieces in R0: element (q, k) of piece i at i*16K + (k/64)*8K +
-        // sw128_off(q, k % 64); k < 64: Re E[k][q], k >= 64: -Im E[k-64][q].
-        // Task (q, k-group of 8): 64 x 16 = 1024 tasks, 4 each.
-        __syncthreads();
+    if (rotated) {
+        uint4 pv[4];
+        load_rot_piece(pv, P, pplane, ax.col, lslot, 0, 2, tid);   // overlaps the B build
+        __syncthreads();                                   // the diagonal above is read
+        // B pieces at [0, 48K): element (q, k) of piece i at i*16K + (k/64)*8K
+        // + sw128_off(q, k % 64); k < 64: Re E[k][q], k >= 64: -Im E[k-64][q].
+        // Task (q, k-group of 8): 64 x 16 = 1024 tasks, 4 a thread.
 #pragma unroll 1
         for (int h = 0; h < 4; ++h) {
             const int task = tid + TJ_T * h;
@@ -440,37 +463,42 @@ tc_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, doub
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
                 const int k = kg * 8 + e;
-                const cf x = Q[(k & 63) * TJ_QS + q];
+                const cf x = E[(k & 63) * TJ_W + q];
                 v[e] = k < 64 ? x.x : -x.y;
             }
-            put_pieces(R0, TJ_PIECE, (uint32_t)(kg >> 3) * 8192u + tc::sw128_off(q, (kg & 7) * 8), v);
+            put_pieces(smem, TJ_PIECE, (uint32_t)(kg >> 3) * 8192u + tc::sw128_off(q, (kg & 7) * 8), v);
         }
-        __syncthreads();                                   // E (R1) is dead
+        __syncthreads();                                   // E is dead
+        uint8_t* At = smem + TJ_AOFF;
         constexpr uint32_t IDESC_R = tc::idesc_bf16(128, 64, true, false);
         const int npair = lslot / 64;
-        float y[4][8];
-        load_rot_chunk(y, X, ax.col, lslot, 0, tid);
+        // the epilogue's elements: real mreal of the chunk, columns q0..q0+31
+        const int mreal = 32 * (warp & 3) + lane;
+        const int q0 = 32 * (warp >> 2);
+        const uint8_t* xsrc = At + (uint32_t)(mreal >> 6) * TJ_PIECE;
+        // Y of the epilogue's elements, summed from the pieces as they pass
+        // through the tile, is parked in TMEM columns 64..127 (the MMAs use
+        // 0..63) between the steps
+        const uint32_t tpark = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 64u + (uint32_t)q0;
         for (int cp = 0; ok && cp < npair; ++cp) {
-            // piece products smallest first: A2 B0 | A1 B1, A1 B0 | A0 B2, A0 B1,
-            // A0 B0, each over all eight K steps, so that only the last eight
-            // MMAs see a full-size accumulator
-            for (int step = 0; step < 3 && ok; ++step) {
+            // piece products smallest first: A2 B0 | A1 B1, A1 B0 | A0 B2,
+            // A0 B1, A0 B0, each over all eight K steps
+            for (int step = 0; step < 3; ++step) {
                 const int ia = 2 - step;
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
-                    const int task = tid + TJ_T * h;
-                    const int p = task >> 4, grp = task & 15;
-                    const uint32_t mo = (uint32_t)(grp >> 3) * TJ_PIECE;
-                    float t[8];
-                    twist8(y[h], t);
-                    put_piece(R1, mo + tc::sw128_off(p, (grp & 7) * 8), y[h], ia);
-                    put_piece(R1, mo + tc::sw128_off(TJ_W + p, (grp & 7) * 8), t, ia);
+                    const int t = tid + TJ_T * h;
+                    const int p = t >> 4, gg = t & 15;
+                    const uint32_t mo = (uint32_t)(gg >> 3) * TJ_PIECE;
+                    *reinterpret_cast<uint4*>(At + mo + tc::sw128_off(p, (gg & 7) * 8)) = pv[h];
+                    *reinterpret_cast<uint4*>(At + mo + tc::sw128_off(TJ_W + p, (gg & 7) * 8)) =
+                        twist_packed(pv[h]);
                 }
                 tc::fence_async_smem();
                 __syncthreads();
                 if (tid == 0) {
                     tc::fence_after_sync();
-                    const uint32_t sa = tc::smem_u32(R1), sb = tc::smem_u32(R0);
+                    const uint32_t sa = tc::smem_u32(At), sb = tc::smem_u32(smem);
                     for (int ib = 2 - ia; ib >= 0; --ib)
 #pragma unroll 1
                         for (int ks = 0; ks < 8; ++ks)
@@ -478,30 +506,46 @@ tc_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, doub
                                          tc::sdesc(sb + ib * TJ_PIECE + (ks >> 2) * 8192 +
                                                        (ks & 3) * 32, 16, 1024),
                                          IDESC_R, (step | ks | (ib != 2 - ia)) != 0);
-                    tc::mma_commit(&ax.bar);
+                    tc::mma_commit(&ax.bar[0]);
                 }
-                if (step == 2 && cp + 1 < npair) {
-                    // the current values were written for the last time: the
-                    // next chunk's loads overlap the last MMAs
-                    load_rot_chunk(y, X, ax.col, lslot, cp + 1, tid);
+                // this piece of the epilogue's elements, from the tile (the
+                // sum p2 + p1 + p0 is exact in any order of these steps)
+                {
+                    float xacc[32];
+                    if (step > 0) tc::tmem_ld32(tpark, xacc);
+#pragma unroll
+                    for (int e = 0; e < 32; ++e) {
+                        const float x = bf16_bits(*reinterpret_cast<const uint16_t*>(
+                            xsrc + tc::sw128_off(q0 + e, mreal & 63)));
+                        xacc[e] = step == 0 ? x : xacc[e] + x;
+                    }
+                    tc::tmem_st32(tpark, xacc);
                 }
-                ok = __syncthreads_and(wait_mma(&ax.bar, phase)) != 0;
+                // the next piece's loads overlap the MMAs
+                if (step < 2)
+                    load_rot_piece(pv, P, pplane, ax.col, lslot, cp, ia - 1, tid);
+                else if (cp + 1 < npair)
+                    load_rot_piece(pv, P, pplane, ax.col, lslot, cp + 1, 2, tid);
+                ok = __syncthreads_and(wait_mma(&ax.bar[0], ph0)) != 0;
+                if (!ok) break;
             }
             if (!ok) break;
             tc::fence_after_sync();
-            // epilogue: lane = real index within the 128 reals of rows 64cp..;
-            // Y + D with FP32 round-to-nearest
-            {
-                const int mreal = 32 * (warp & 3) + lane;
-                const int q0 = 32 * (warp >> 2);
-                float v[32];
-                tc::tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + q0, v);
+            // epilogue: Y + D in FP32 with round-to-nearest, then its pieces
 #pragma unroll
-                for (int e = 0; e < 32; ++e) {
-                    const int col = ax.col[q0 + e];
+            for (int half = 0; half < 2; ++half) {
+                float v[16], xacc[16];
+                tc::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + q0 + 16 * half, v);
+                tc::tmem_ld16(tpark + 16 * half, xacc);
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int col = ax.col[q0 + 16 * half + e];
                     if (col >= 0) {
-                        float* dst = X + ((size_t)col * lslot + (size_t)cp * 64) * 2 + mreal;
-                        *dst = __ldcg(dst) + v[e];
+                        const size_t off = (size_t)col * 2 * lslot + (size_t)cp * 128 + mreal;
+                        const tc::Split3 sp = tc::split3(xacc[e] + v[e]);
+                        P[off] = __bfloat16_as_ushort(sp.p0);
+                        P[pplane + off] = __bfloat16_as_ushort(sp.p1);
+                        P[2 * pplane + off] = __bfloat16_as_ushort(sp.p2);
                     }
                 }
             }
@@ -510,54 +554,294 @@ tc_visit_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int round, doub
             tc::fence_after_sync();
         }
     }
-    if (!ok && tid == 0) atomicExch(g.counter + 3, 1);     // an MMA wait expired
     if (tid == 0) {
         const long long c3 = clock64();
         atomicAdd(&g_tj_cycles[0], (unsigned long long)(c1 - c0));
         atomicAdd(&g_tj_cycles[1], (unsigned long long)(c2 - c1));
         atomicAdd(&g_tj_cycles[2], (unsigned long long)(c3 - c2));
         atomicAdd(&g_tj_cycles[3], 1ull);
+        if (rotated) {
+            atomicAdd(&g_tj_cycles[4], 1ull);
+            atomicAdd(&g_tj_cycles[5], (unsigned long long)rsteps);
+            atomicAdd(&g_tj_cycles[6], (unsigned long long)rpairs);
+        }
+    }
+    return rotated;
+}
+
+// One persistent launch per sweep: CTAs claim the visits (round, job, block
+// pair) in round-major order from one counter, wait (bounded) until both
+// blocks have finished the previous round, run the visit and publish the
+// round -- the protocol of the SIMT sweep kernel, so visits of different
+// rounds and jobs overlap and the two CTAs on an SM are seldom in the same
+// step.  A visit whose pairs were all below the tolerance when it last ran,
+// and whose blocks have not changed since (no rotation touched them and the
+// sort kept their sets of columns), is skipped.  tbase = sweep * (rounds + 1).
+__global__ void __launch_bounds__(TJ_T, 2)
+tc_sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, double tol2d, float tol2,
+                int njobs, int rounds, int pairs, SweepSync sync, int tbase) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                               ~uintptr_t(1023));
+    Aux& ax = *reinterpret_cast<Aux*>(smem + TJ_AUX);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        mbar_init(&ax.bar[0], 1);
+        mbar_init(&ax.bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&ax.tmem, TJ_TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const long long t_start = clock64();
+    const uint32_t tmem = ax.tmem;
+    unsigned ph0 = 0u, ph1 = 0u;     // phases of bar[0], bar[1], kept across visits
+    const int per_round = njobs * pairs;
+    const int total = rounds * per_round;
+    for (;;) {
+        if (tid == 0) {
+            ax.item = atomicAdd(sync.next_item, 1);
+            ax.abort = *reinterpret_cast<volatile int*>(sync.error);
+        }
+        __syncthreads();
+        const int item = ax.item;
+        if (item >= total || ax.abort) break;
+        const int r = item / per_round, rem = item - r * per_round;
+        const int j = rem / pairs, p = rem - (rem / pairs) * pairs;
+        bool active = !g.done[j];
+        int I = 0, J = 0, nb = 2;
+        if (active) {
+            const mps_2q_job job = jobs[j];
+            const int m = job.chi_l * g.d, n = job.chi_r * g.d;
+            const int C = min(m, n);
+            if (job_tracks_v(m, n, job.keep_left_canonical) || C < TJ_W) {
+                // only left-canonical tall jobs of 64+ columns take these sweeps
+                if (tid == 0 && r == 0 && p == 0) atomicExch(g.counter + 2, 1);
+                active = false;
+            } else {
+                nb = (C + TJ_BC - 1) / TJ_BC;
+                nb += nb & 1;
+                active = r < nb - 1 && p < nb / 2;
+                if (active) tournament_pair(nb, r, p, I, J);
+            }
+        }
+        if (active) {
+            // a job of one block pair has one visit per sweep, and a visit
+            // that rotates nothing ends it: no stamps
+            const bool track = nb > 2;
+            volatile int* vst = g.vstamp + (size_t)j * g.nbmax;
+            volatile int* qst = g.qstamp + (size_t)j * g.qstride + r * pairs + p;
+            if (tid == 0) {
+                // qstamp of this (round, pair) changes only when this item
+                // runs, so it is read before the wait; the block stamps after it
+                const int q = track ? *qst : -1;
+                ax.skip = 0;
+                if (r > 0) {
+                    const long long w0 = clock64();
+                    volatile int* fl = sync.block_round + (size_t)j * sync.nbmax;
+                    volatile int* err = sync.error;
+                    int polls = 0;
+                    while ((fl[I] < r - 1 || fl[J] < r - 1) && *err == 0) {
+                        if (++polls > sync.wait_limit) {
+                            atomicExch(sync.error, 1);
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                    ax.abort = *err;
+                    __threadfence();
+                    atomicAdd(&g_tj_cycles[7], (unsigned long long)(clock64() - w0));
+                }
+                if (track) ax.skip = (q >= 0 && q > vst[I] && q > vst[J]) ? 1 : 0;
+            }
+            __syncthreads();
+            if (ax.abort) break;
+            bool rot = false;
+            if (!ax.skip) {
+                bool ok = true;
+                rot = visit(g, j, I, J, r == 0, tol2d, tol2, smem, ax, tmem, ph0, ph1, ok);
+                if (!ok) {
+                    // an MMA wait expired: stop every CTA (the call reports it)
+                    if (tid == 0) {
+                        atomicExch(g.counter + 3, 1);
+                        atomicExch(sync.error, 1);
+                    }
+                    break;
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                if (track && !ax.skip) {
+                    const int now = tbase + r + 1;
+                    if (rot) {
+                        vst[I] = now;
+                        vst[J] = now;
+                    } else {
+                        *qst = now;
+                    }
+                }
+                __threadfence();
+                atomicExch(sync.block_round + (size_t)j * sync.nbmax + I, r);
+                atomicExch(sync.block_round + (size_t)j * sync.nbmax + J, r);
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        atomicAdd(&g_tj_cycles[8], (unsigned long long)(clock64() - t_start));
+        atomicAdd(&g_tj_cycles[9], 1ull);
     }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, TJ_TMEM_COLS);
 }
 
+// X <-> its three bf16 piece planes, every element of every job's slot, 8
+// reals a thread (a slot holds 2 lslot cslot reals, a multiple of 64).
+__global__ void __launch_bounds__(256) tc_split_kernel(TwoQGeom g, int njobs) {
+    const size_t per8 = g.pplane / 8;
+    const size_t total8 = per8 * (size_t)njobs;
+    const float4* X = reinterpret_cast<const float4*>(g.X);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total8;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t jj = e / per8, off = (e - jj * per8) * 8;
+        const float4 lo = __ldcs(X + 2 * e), hi = __ldcs(X + 2 * e + 1);
+        const float v[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+        uint8_t* base = reinterpret_cast<uint8_t*>(g.P + jj * 3 * g.pplane + off);
+        put_pieces(base, g.pplane * sizeof(uint16_t), 0u, v);
+    }
+}
+
+__global__ void __launch_bounds__(256) tc_merge_kernel(TwoQGeom g, int njobs) {
+    const size_t per8 = g.pplane / 8;
+    const size_t total8 = per8 * (size_t)njobs;
+    float4* X = reinterpret_cast<float4*>(g.X);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total8;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t jj = e / per8, off = (e - jj * per8) * 8;
+        const uint16_t* base = g.P + jj * 3 * g.pplane + off;
+        const uint4 w0 = __ldcs(reinterpret_cast<const uint4*>(base));
+        const uint4 w1 = __ldcs(reinterpret_cast<const uint4*>(base + g.pplane));
+        const uint4 w2 = __ldcs(reinterpret_cast<const uint4*>(base + 2 * g.pplane));
+        const uint32_t a0[4] = {w0.x, w0.y, w0.z, w0.w};
+        const uint32_t a1[4] = {w1.x, w1.y, w1.z, w1.w};
+        const uint32_t a2[4] = {w2.x, w2.y, w2.z, w2.w};
+        float v[8];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            // the sum is exact: p1 + p2 is the first residual, p0 + it is x
+            v[2 * k] = __uint_as_float(a0[k] << 16) +
+                       (__uint_as_float(a1[k] << 16) + __uint_as_float(a2[k] << 16));
+            v[2 * k + 1] = __uint_as_float(a0[k] & 0xffff0000u) +
+                           (__uint_as_float(a1[k] & 0xffff0000u) + __uint_as_float(a2[k] & 0xffff0000u));
+        }
+        __stcs(X + 2 * e, make_float4(v[0], v[1], v[2], v[3]));
+        __stcs(X + 2 * e + 1, make_float4(v[4], v[5], v[6], v[7]));
+    }
+}
+
+int split_grid(const TwoQGeom& g, int njobs) {
+    const size_t total8 = g.pplane / 8 * (size_t)njobs;
+    return (int)std::min<size_t>((total8 + 255) / 256, 152 * 8);
+}
+
 }  // namespace
 
+int tc_split_launch(int njobs, const TwoQGeom& g, cudaStream_t s) {
+    if (!g.P) return fail(MPS_ERR_ARG, "tc sweeps: the workspace has no piece planes");
+    if (g.pplane % 64 != 0) return fail(MPS_ERR_ARG, "tc sweeps: unsupported slot size");
+    tc_split_kernel<<<split_grid(g, njobs), 256, 0, s>>>(g, njobs);
+    MPS_LAUNCH_CHECK("tc_split_kernel");
+    return MPS_OK;
+}
+
+int tc_merge_launch(int njobs, const TwoQGeom& g, cudaStream_t s) {
+    if (!g.P) return fail(MPS_ERR_ARG, "tc sweeps: the workspace has no piece planes");
+    if (g.pplane % 64 != 0) return fail(MPS_ERR_ARG, "tc sweeps: unsupported slot size");
+    tc_merge_kernel<<<split_grid(g, njobs), 256, 0, s>>>(g, njobs);
+    MPS_LAUNCH_CHECK("tc_merge_kernel");
+    return MPS_OK;
+}
+
 int tc_sweep_launch(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const TwoQGeom& g,
-                    float tol2, cudaStream_t s) {
+                    float tol2, const SweepSync& sync, int tbase, cudaStream_t s) {
     static KernelSetup ks;
     int dev = 0;
     MPS_CUDA_CHECK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return fail(MPS_ERR_ARG, "device index beyond 63");
     std::call_once(ks.once[dev], [&] {
-        cudaError_t e = cudaFuncSetAttribute(tc_visit_kernel,
+        int rc = MPS_OK;
+        cudaError_t e = cudaFuncSetAttribute(tc_sweep_kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)TJ_SMEM);
-        ks.rc[dev] = e == cudaSuccess ? MPS_OK : cuda_fail(e, "cudaFuncSetAttribute(tc_visit_kernel)");
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaFuncSetAttribute(tc_sweep_kernel)");
+        // all of the unified L1 as shared memory: two CTAs of ~100 KB per SM
+        // (with the default split the occupancy is one)
+        if (rc == MPS_OK) {
+            e = cudaFuncSetAttribute(tc_sweep_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
+            if (e != cudaSuccess) rc = cuda_fail(e, "carveout of tc_sweep_kernel");
+        }
+        int sms = 0, per_sm = 0;
+        if (rc == MPS_OK) {
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_sweep_kernel, TJ_T, TJ_SMEM);
+            if (e != cudaSuccess) rc = cuda_fail(e, "resident CTAs of tc_sweep_kernel");
+        }
+        // The occupancy query answers 1 for this kernel even without dynamic
+        // shared memory; by its registers and shared memory two CTAs fit (and
+        // do run side by side).  A larger grid is safe either way: a visit
+        // only waits for visits that running CTAs claimed before it.
+        if (rc == MPS_OK) {
+            cudaFuncAttributes fa;
+            e = cudaFuncGetAttributes(&fa, tc_sweep_kernel);
+            if (e != cudaSuccess) rc = cuda_fail(e, "attributes of tc_sweep_kernel");
+            int regs_per_sm = 0, smem_per_sm = 0, smem_reserved = 0;
+            if (rc == MPS_OK) {
+                cudaDeviceGetAttribute(&regs_per_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+                cudaDeviceGetAttribute(&smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+                cudaDeviceGetAttribute(&smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+                const int by_regs = regs_per_sm / std::max(1, ((fa.numRegs * 32 + 255) / 256) * 256 * (TJ_T / 32));
+                const int by_smem = smem_per_sm / (int)(TJ_SMEM + fa.sharedSizeBytes + smem_reserved);
+                per_sm = std::max(per_sm, std::min(by_regs, by_smem));
+            }
+        }
+        // every CTA allocates TMEM_COLS of the SM's 512 TMEM columns
+        per_sm = std::min(per_sm, (int)(512 / TJ_TMEM_COLS));
+        ks.ctas[dev] = sms * (per_sm > 0 ? per_sm : 1);
+        ks.rc[dev] = rc;
     });
     if (ks.rc[dev] != MPS_OK) return ks.rc[dev];
     if (g.lslot % 64 != 0) return fail(MPS_ERR_ARG, "tc sweeps: slot rows must be a multiple of 64");
-    for (int r = 0; r < rounds; ++r) {
-        tc_visit_kernel<<<dim3(pairs, njobs), TJ_T, TJ_SMEM, s>>>(jobs, g, r, (double)tol2, tol2);
-        MPS_LAUNCH_CHECK("tc_visit_kernel");
-    }
+    if (!g.P) return fail(MPS_ERR_ARG, "tc sweeps: the workspace has no piece planes");
+    if (!g.vstamp || !g.qstamp) return fail(MPS_ERR_ARG, "tc sweeps: no visit stamps");
+    const int total = rounds * njobs * pairs;
+    if (total <= 0) return MPS_OK;
+    // co-resident CTAs only: a visit waits for visits claimed before it
+    const int grid = std::min(total, ks.ctas[dev]);
+    tc_sweep_kernel<<<grid, TJ_T, TJ_SMEM, s>>>(jobs, g, (double)tol2, tol2, njobs, rounds, pairs,
+                                                sync, tbase);
+    MPS_LAUNCH_CHECK("tc_sweep_kernel");
     return MPS_OK;
 }
 
 }  // namespace mps
 
-// Per-step cycle totals of the tensor-core visits (see g_tj_cycles); reset
-// after reading when reset != 0.  Blocks.
-extern "C" int mps_tc_profile(unsigned long long* out4, int reset) {
-    unsigned long long v[4] = {0, 0, 0, 0};
+// Counters of the tensor-core visits (g_tj_cycles), reset after reading when
+// reset != 0.  Blocks.
+extern "C" int mps_tc_profile(unsigned long long* out10, int reset) {
+    unsigned long long v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     MPS_CUDA_CHECK(cudaMemcpyFromSymbol(v, mps::g_tj_cycles, sizeof(v)));
     if (reset) {
-        const unsigned long long z[4] = {0, 0, 0, 0};
+        const unsigned long long z[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         MPS_CUDA_CHECK(cudaMemcpyToSymbol(mps::g_tj_cycles, z, sizeof(z)));
     }
-    if (out4)
-        for (int i = 0; i < 4; ++i) out4[i] = v[i];
+    if (out10)
+        for (int i = 0; i < 10; ++i) out10[i] = v[i];
     return MPS_OK;
 }

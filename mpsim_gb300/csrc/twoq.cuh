@@ -38,6 +38,12 @@ struct TwoQGeom {
     int* vstamp;      // njobs * nbmax: last time a column block changed
     int* qstamp;      // njobs * qstride: last time visit (round, pair) rotated nothing
     int nbmax, qstride;
+    // MPS_PRECISION_MIXED only (null otherwise): X split into three bf16
+    // piece planes per job, plane i of job j at P + (3 j + i) * pplane, each
+    // laid out like X (column c = 2 lslot bf16 at c * 2 lslot); during the
+    // tensor-core sweeps the planes, not X, hold the columns
+    uint16_t* P;
+    size_t pplane;
 };
 
 // Work distribution of the persistent sweep kernel.
@@ -66,11 +72,17 @@ constexpr float kZeroSigma = 1e-30f;
 int lq_precondition(const mps_2q_job* jobs, int njobs, int max_m, int max_n, const TwoQGeom& g,
                     cudaStream_t s);
 
-// Tensor-core block sweeps (tcjacobi.cu): every round of one sweep of the
-// left-canonical tall jobs, 32-column blocks.  counter[2] is set when a job
-// of another kind was given, counter[3] when a bounded MMA wait expired.
+// Tensor-core block sweeps (tcjacobi.cu): one persistent launch runs every
+// round of one sweep of the left-canonical tall jobs, 32-column blocks, with
+// the sweep kernel's round flags (sync) and visit stamps (tbase = sweep *
+// (rounds + 1)).  counter[2] is set when a job of another kind was given,
+// counter[3] (and sync.error) when a bounded MMA wait expired.
 int tc_sweep_launch(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const TwoQGeom& g,
-                    float tol2, cudaStream_t s);
+                    float tol2, const SweepSync& sync, int tbase, cudaStream_t s);
+// X -> its bf16 piece planes (before the first tensor-core sweep).
+int tc_split_launch(int njobs, const TwoQGeom& g, cudaStream_t s);
+// The piece planes summed back into X (after the last tensor-core sweep).
+int tc_merge_launch(int njobs, const TwoQGeom& g, cudaStream_t s);
 
 int merge_gate_launch(const mps_2q_job* jobs, int njobs, int max_chil, int max_chir,
                       const TwoQGeom& g, cudaStream_t s);

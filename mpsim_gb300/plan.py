@@ -238,7 +238,9 @@ class CircuitPlan:
         ws = 1
         for cl in calls:
             if cl[0] == "2q":
-                ws = max(ws, int(self.lib.mps_2q_workspace_bytes(cl[2], cl[3], cl[4], d)))
+                size_fn = (self.lib.mps_2q_workspace_bytes_mixed
+                           if cl[5] == _native.PRECISION_MIXED else self.lib.mps_2q_workspace_bytes)
+                ws = max(ws, int(size_fn(cl[2], cl[3], cl[4], d)))
         self.workspace = torch.empty(ws, dtype=torch.uint8, device=self.device)
         self._final = [[(o, shp) for (o, shp) in cur[ci]] for ci in range(len(self.circuits))]
         self._params = _native.SvdParams()

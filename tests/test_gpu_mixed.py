@@ -131,6 +131,23 @@ def test_mixed_rejects_other_jobs(built_lib, cuda):
     assert rc == 0, _native.last_error()
 
 
+def test_mixed_needs_its_workspace_size(built_lib, cuda):
+    """A mixed call given only the plain form's workspace (no room for the
+    piece planes) is refused before any launch."""
+    import ctypes
+    rng = np.random.default_rng(4)
+    a, b, g = make_job_inputs(rng, 64, 64, 64, 2)
+    small = built_lib.mps_2q_workspace_bytes(1, 128, 128, 2)
+    assert built_lib.mps_2q_workspace_bytes_mixed(1, 128, 128, 2) > small
+    ws = torch.empty(small, dtype=torch.uint8, device=cuda)
+    jobs = torch.zeros(_native.JOB_DTYPE.itemsize, dtype=torch.uint8, device=cuda)
+    p = mixed_params()
+    rc = built_lib.mps_apply_2q_batch(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream),
+                                      ctypes.c_void_p(jobs.data_ptr()), 1, 128, 128, 2,
+                                      ctypes.c_void_p(ws.data_ptr()), small, ctypes.byref(p))
+    assert rc == _native.MPS_ERR_WORKSPACE
+
+
 def test_mixed_circuit_10q_matches_reference_complex128(built_lib, cuda):
     """The 10-qubit depth-10 untruncated workload with precision="mixed"
     (its merged matrices are at most 32 x 32, so every gate takes the plain

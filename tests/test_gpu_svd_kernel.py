@@ -67,9 +67,11 @@ def run_batch(lib, dev, specs, params=None):
         row["keep_left_canonical"] = int(lc)
         max_m, max_n = max(max_m, chil * d), max(max_n, chir * d)
     jobs = torch.from_numpy(table.view(np.uint8)).to(dev)
-    nbytes = lib.mps_2q_workspace_bytes(njobs, max_m, max_n, d)
-    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
     p = params or _native.SvdParams()
+    size_fn = (lib.mps_2q_workspace_bytes_mixed if p.precision == _native.PRECISION_MIXED
+               else lib.mps_2q_workspace_bytes)
+    nbytes = size_fn(njobs, max_m, max_n, d)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     rc = lib.mps_apply_2q_batch(stream, ctypes.c_void_p(jobs.data_ptr()), njobs, max_m, max_n, d,
                                 ctypes.c_void_p(ws.data_ptr()), nbytes, ctypes.byref(p))

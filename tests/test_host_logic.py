@@ -148,6 +148,10 @@ def test_library_exports_every_header_symbol(built_lib):
     assert built_lib.mps_version() >= 100
     assert built_lib.mps_2q_workspace_bytes(0, 4, 4, 2) == 0
     assert built_lib.mps_2q_workspace_bytes(32, 512, 512, 2) >= 32 * 2 * 512 * 512 * 8
+    # the mixed form adds three bf16 piece planes (12 bytes a complex element)
+    assert (built_lib.mps_2q_workspace_bytes_mixed(32, 512, 512, 2)
+            >= built_lib.mps_2q_workspace_bytes(32, 512, 512, 2) + 32 * 512 * 512 * 12)
+    assert built_lib.mps_2q_workspace_bytes_mixed(0, 4, 4, 2) == 0
 
 
 def test_job_struct_layout_matches_header(tmp_path):
