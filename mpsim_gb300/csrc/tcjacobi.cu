@@ -50,16 +50,18 @@
 //                two columns, warp w: rows w, w + 8, ...): H = G R written
 //                conjugate-transposed, then G' = H^H R (G is Hermitian); E
 //                takes R in the second pass.
-//   3. Update:   Y <- Y + Y E, skipped when the visit rotated nothing.  The
-//                tensor cores form D = Y E from piece tiles of Y read as an
-//                MN-major A operand (M = 128 reals of the column, K = the 128
-//                tile rows) times a K-major B holding (Re E, -Im E); the
-//                epilogue adds D to Y (summed from its pieces) in FP32 with
-//                round-to-nearest and writes the new pieces.  The update form
-//                keeps the truncation small: D = Y E is small once the
-//                rotations are (accumulating Y Q in full shrank every singular
-//                value by ~5e-5 over a chi=256 SVD).  The piece products are
-//                issued smallest first.
+//   3. Update:   Y <- Y + Y E, skipped when the visit rotated nothing.  Per
+//                64 rows, the tensor cores form D1 = Y Re E and D2 = Y Im E
+//                from the rows' piece tiles read as an MN-major A operand
+//                (M = the 128 interleaved reals, K = the 64 visit columns)
+//                times a K-major B holding Re E and Im E (N = 128); the
+//                epilogue combines the two reals of a row (adjacent TMEM
+//                lanes, one shuffle), adds the result to Y (summed from its
+//                pieces) in FP32 with round-to-nearest and writes the new
+//                pieces.  The update form keeps the truncation small: D = Y E
+//                is small once the rotations are (accumulating Y Q in full
+//                shrank every singular value by ~5e-5 over a chi=256 SVD).
+//                The piece products are issued smallest first.
 // The new squared column norms (the diagonal of Q^H G Q) go to cnrm for the
 // next sweep's sort.
 //
@@ -70,7 +72,8 @@
 //   [32K, 64K) step 2: H^H, the first pass's output (same layout)
 //   [64K, 96K) step 2: E = Q - I (64 x 64 complex, row-major)
 //   [0, 48K)   step 3: the three B-operand pieces of E (16 KB each)
-//   [48K, 80K) step 3: one A piece tile (two 16 KB M-groups)
+//   [48K, 96K) step 3: the three A piece tiles of 64 rows (two 8 KB M-groups
+//              each), filled by cp.async
 #include "rot.cuh"
 #include "tc.cuh"
 #include "twoq.cuh"
@@ -86,12 +89,13 @@ constexpr uint32_t TJ_GTILE = 3 * TJ_PIECE;         // one Gram tile buffer (48 
 constexpr uint32_t TJ_GBUF = TJ_W * TJ_W * 8;       // one 64 x 64 complex buffer (32 KB)
 constexpr uint32_t TJ_HOFF = TJ_GBUF;               // H^H at 32 KB
 constexpr uint32_t TJ_EOFF = 2 * TJ_GBUF;           // E at 64 KB
-constexpr uint32_t TJ_AOFF = 3 * TJ_PIECE;          // the update's A tile at 48 KB
+constexpr uint32_t TJ_AOFF = 3 * TJ_PIECE;          // the update's A tiles at 48 KB
+constexpr uint32_t TJ_MGRP = 8192;                  // one 64-real M-group of an A tile
 constexpr uint32_t TJ_AUX = 2 * TJ_GTILE;           // 96 KB: small arrays
 constexpr uint32_t TJ_TMEM_COLS = 128;              // two 64-column Gram accumulators
 constexpr int TJ_WAIT_LIMIT = 1 << 14;
 static_assert(TJ_EOFF + TJ_GBUF <= TJ_AUX, "E overlaps the small arrays");
-static_assert(TJ_AOFF + 2 * TJ_PIECE <= TJ_AUX, "the update's A tile overlaps the small arrays");
+static_assert(TJ_AOFF + 3 * TJ_PIECE <= TJ_AUX, "the update's A tiles overlap the small arrays");
 
 // Cycles spent in the three steps of a visit, summed over the CTAs of every
 // visit since the last reset: [0] Gram, [1] rotations on G, [2] Y <- Y + Y E,
@@ -108,6 +112,7 @@ struct Aux {
     int rotated;          // some pair of this visit needs a rotation
     int col[TJ_W];        // physical column of each visit column (-1: zero padding)
     float diag[TJ_W];     // diagonal of G (squared column norms)
+    cf gam[TJ_W / 2];     // G[cP][cQ] of the 32 pairs of the next inner step
     float cmax;           // largest squared cosine of the visit's pairs
 };
 constexpr size_t TJ_SMEM = TJ_AUX + sizeof(Aux) + 1024;
@@ -123,25 +128,63 @@ __device__ __forceinline__ bool wait_mma(uint64_t* bar, unsigned& phase) {
     return ok;
 }
 
-// Pair k of inner step s: the 32 x 32 inter-block pairs (ring) or the
-// circle-method pairs of all 64 columns (full).
-__device__ __forceinline__ void inner_pair(bool full, int s, int k, int& p, int& q) {
-    if (full) {
-        tournament_pair(TJ_W, s, k, p, q);
-    } else {
-        p = k;
-        q = TJ_BC + ((k + s) & (TJ_BC - 1));
-    }
+// Columns x (p) and y (q) of a row times R = [[1 - tp, conj(s)], [-s, 1 - tp]]
+// in the tau form of rot.cuh: x' = x - (tp x + s y), y' = y + (conj(s) x -
+// tp y).  Twelve FMAs; each output starts from fma(-tp, x, x), which rounds
+// x - tp x once (an explicit c = 1 - tp would round to 1 for small angles and
+// inflate the norms).
+__device__ __forceinline__ void rotate_cols(cf& x, cf& y, float tp, cf sg) {
+    const float xr = x.x, xi = x.y, yr = y.x, yi = y.y;
+    x.x = fmaf(-sg.x, yr, fmaf(sg.y, yi, fmaf(-tp, xr, xr)));
+    x.y = fmaf(-sg.x, yi, fmaf(-sg.y, yr, fmaf(-tp, xi, xi)));
+    y.x = fmaf(sg.x, xr, fmaf(sg.y, xi, fmaf(-tp, yr, yr)));
+    y.y = fmaf(sg.x, xi, fmaf(-sg.y, xr, fmaf(-tp, yi, yi)));
 }
 
-// Columns x (p) and y (q) of a row times R = [[1 - tp, conj(s)], [-s, 1 - tp]]
-// in the tau form of rot.cuh (an explicit c = 1 - tp would round to 1 for
-// small angles and inflate the norms).
-__device__ __forceinline__ void rotate_cols(cf& x, cf& y, float tp, cf sg) {
-    const cf nx = csub(x, cadd(cscale(x, tp), cmul(y, sg)));
-    const cf ny = cadd(y, csub(cmul(x, cconj(sg)), cscale(y, tp)));
-    x = nx;
-    y = ny;
+__device__ __forceinline__ cf shfl_cf(cf v, int src) {
+    return cmake(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// One step of the circle method over the 32 lanes' (top, bottom) slots:
+// top of lane 0 stays, top of lane 1 <- bottom of lane 0, top of lane k <-
+// top of lane k - 1 (k >= 2), bottom of lane k <- bottom of lane k + 1
+// (k <= 30), bottom of lane 31 <- top of lane 31.
+__device__ __forceinline__ float circle_top(float t, float b, int lane) {
+    const float up = __shfl_up_sync(0xffffffffu, t, 1);
+    const float b0 = __shfl_sync(0xffffffffu, b, 0);
+    return lane == 0 ? t : (lane == 1 ? b0 : up);
+}
+__device__ __forceinline__ float circle_bottom(float t, float b, int lane) {
+    const float dn = __shfl_down_sync(0xffffffffu, b, 1);
+    return lane == 31 ? t : dn;
+}
+__device__ __forceinline__ void circle_move(cf& t, cf& b, int lane) {
+    const cf nt = cmake(circle_top(t.x, b.x, lane), circle_top(t.y, b.y, lane));
+    const cf nb = cmake(circle_bottom(t.x, b.x, lane), circle_bottom(t.y, b.y, lane));
+    t = nt;
+    b = nb;
+}
+__device__ __forceinline__ void circle_move_idx(int& t, int& b, int lane) {
+    const int up = __shfl_up_sync(0xffffffffu, t, 1);
+    const int b0 = __shfl_sync(0xffffffffu, b, 0);
+    const int dn = __shfl_down_sync(0xffffffffu, b, 1);
+    const int nt = lane == 0 ? t : (lane == 1 ? b0 : up);
+    b = lane == 31 ? t : dn;
+    t = nt;
+}
+
+// gamma = G[cP][cQ] of this lane's pair, written by the warp holding row cP
+// (row warp + 8h of gQ).  A masked sum, not an indexed read: an index that
+// depends on the lane would move the array to local memory.
+__device__ __forceinline__ void publish_gamma(const cf (&gQ)[8], int warp, int cP, cf* dst) {
+    cf v = cmake(0.f, 0.f);
+#pragma unroll
+    for (int h = 0; h < 8; ++h) {
+        const float m = (warp + 8 * h == cP) ? 1.f : 0.f;
+        v.x = fmaf(m, gQ[h].x, v.x);
+        v.y = fmaf(m, gQ[h].y, v.y);
+    }
+    if (warp == (cP & 7)) *dst = v;
 }
 
 // T = -i Y on 8 packed bf16 (four (re, im) pairs, re in the low half of each
@@ -207,22 +250,22 @@ __device__ __forceinline__ void load_gram_pieces(uint4 (&v)[6], const uint16_t* 
     }
 }
 
-// Step-3 loads of piece `ia` of rows 64cp..64cp+63 (128 reals, 256 bytes a
-// column): task t (0..1023) = (column p, 16-byte chunk g), 4 a thread.
-__device__ __forceinline__ void load_rot_piece(uint4 (&v)[4], const uint16_t* P, size_t pplane,
-                                               const int* col, int lslot, int cp, int ia, int tid) {
+// Step-3 loads of rows 64cp..64cp+63 (128 reals, 256 bytes a piece column)
+// straight into the A tiles by cp.async: task t (0..3071) = (piece i, column
+// p, 16-byte chunk g), 12 a thread; zero padding for absent columns.
+__device__ __forceinline__ void load_update_pieces(uint8_t* At, const uint16_t* P, size_t pplane,
+                                                   const int* col, int lslot, int cp, int tid) {
 #pragma unroll
-    for (int h = 0; h < 4; ++h) {
+    for (int h = 0; h < 12; ++h) {
         const int t = tid + TJ_T * h;
-        const int p = t >> 4, g = t & 15;
+        const int i = t >> 10, p = (t >> 4) & 63, g = t & 15;
         const int cc = col[p];
-        if (cc >= 0) {
-            const uint16_t* src = P + ia * pplane + (size_t)cc * 2 * lslot + (size_t)cp * 128 + g * 8;
-            v[h] = __ldcg(reinterpret_cast<const uint4*>(src));
-        } else {
-            v[h] = make_uint4(0u, 0u, 0u, 0u);
-        }
+        const uint16_t* src = P + i * pplane + (size_t)(cc >= 0 ? cc : 0) * 2 * lslot +
+                              (size_t)cp * 128 + g * 8;
+        uint8_t* dst = At + i * TJ_PIECE + (uint32_t)(g >> 3) * TJ_MGRP + tc::sw128_off(p, (g & 7) * 8);
+        tc::cp_async16(dst, src, cc >= 0 ? 16u : 0u);
     }
+    tc::cp_async_commit();
 }
 
 // Adds the 32 TMEM columns at taddr (this thread's lane) into acc.
@@ -372,67 +415,118 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
     const bool work = ax.rotated != 0;
     const int nsteps = full ? TJ_W - 1 : TJ_BC;
     int rsteps = 0, rpairs = 0;
-    for (int s = 0; work && s < nsteps; ++s) {
-        // this warp's copy of the step's 32 rotations: lane k holds pair k
-        int p, q;
-        inner_pair(full, s, lane, p, q);
-        float tp = 0.f;
-        cf sg = cmake(0.f, 0.f);
-        bool rot;
-        {
-            const float a = ax.diag[p], b = ax.diag[q];
-            const cf gam = G[gidx(p, q)];
-            // per-step rotation decision in FP32 (the SIMT form's test)
-            rot = pair_cos2(gam, cabs2(gam), a, b) > tol2;
-            if (rot) {
-                const Rot r = make_rot(a, b, gam);
-                tp = r.tp;
-                sg = r.sigma;
-            }
-        }
-        // every warp holds the same 32 decisions: a step without a rotation
-        // is skipped by all of them
-        const unsigned rmask = __ballot_sync(0xffffffffu, rot);
-        if (!rmask) continue;
-        ++rsteps;
-        rpairs += __popc(rmask);
-        // pass 1: H = G R, stored as H^H
-#pragma unroll 4
-        for (int h = 0; h < TJ_W / 8; ++h) {
+    if (work) {
+        // Register-resident: warp w holds rows w, w + 8, ... of G and E, lane
+        // k the two columns of pair k (visit columns cP, cQ).  The column
+        // rotations of both passes are then local; between the passes H goes
+        // through shared memory conjugate-transposed, and between the steps
+        // the columns move to the lanes of their next pairs by shuffles: the
+        // ring's q-columns shift by one lane, the full visit's 63 steps are
+        // the circle method (cP of lane 0 fixed, the other 63 columns moving
+        // along t1 -> t2 -> ... -> t31 -> b31 -> ... -> b0 -> t1).  The angle
+        // inputs of a step, diag and gamma = G[cP][cQ], come from the warps
+        // holding those rows, through the small arrays.
+        int cP = lane, cQ = full ? TJ_W - 1 - lane : TJ_BC + lane;
+        cf gP[8], gQ[8], eP[8], eQ[8];
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
             const int r = warp + 8 * h;
-            cf x = G[gidx(r, p)], y = G[gidx(r, q)];
-            if (rot) rotate_cols(x, y, tp, sg);
-            H[gidx(p, r)] = cconj(x);
-            H[gidx(q, r)] = cconj(y);
+            gP[h] = G[gidx(r, cP)];
+            gQ[h] = G[gidx(r, cQ)];
+            eP[h] = cmake(0.f, 0.f);
+            eQ[h] = cmake(0.f, 0.f);
         }
+        publish_gamma(gQ, warp, cP, ax.gam + lane);
         __syncthreads();
-        // pass 2: G' = H^H R (= R^H G R), and E <- E R (E = Q - I: the
-        // identity is added back here only)
-#pragma unroll 2
-        for (int h = 0; h < TJ_W / 8; ++h) {
+        for (int s = 0; s < nsteps; ++s) {
+            // this warp's copy of the step's 32 rotations: lane k holds pair k
+            // (tp = sigma = 0 for a pair that does not rotate: the rotation
+            // below is then exactly the identity)
+            float tp = 0.f, na = 0.f, nb = 0.f;
+            cf sg = cmake(0.f, 0.f);
+            bool rot;
+            {
+                const float a = ax.diag[cP], b = ax.diag[cQ];
+                const cf gam = ax.gam[lane];
+                // per-step rotation decision in FP32 (the SIMT form's test)
+                rot = pair_cos2(gam, cabs2(gam), a, b) > tol2;
+                if (rot) {
+                    const Rot r = make_rot(a, b, gam);
+                    tp = r.tp;
+                    sg = r.sigma;
+                    na = a - r.dn;        // the norm transfer of rot.cuh
+                    nb = b + r.dn;
+                }
+            }
+            // every warp holds the same 32 decisions: a step without a
+            // rotation changes nothing
+            const unsigned rmask = __ballot_sync(0xffffffffu, rot);
+            if (rmask) {
+                ++rsteps;
+                rpairs += __popc(rmask);
+                // pass 1: H = G R on this warp's rows, stored as H^H
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    const int r = warp + 8 * h;
+                    rotate_cols(gP[h], gQ[h], tp, sg);
+                    H[gidx(cP, r)] = cconj(gP[h]);
+                    H[gidx(cQ, r)] = cconj(gQ[h]);
+                }
+                __syncthreads();
+                // every warp has read this step's diagonal
+                if (warp == 0 && rot) {
+                    ax.diag[cP] = na;
+                    ax.diag[cQ] = nb;
+                }
+                // pass 2: G' = H^H R (= R^H G R) and E <- (I + E) R - I =
+                // E R + (R - I), whose identity part adds -tp, -sigma to
+                // column cP and conj(sigma), -tp to column cQ in rows cP, cQ.
+                // (The rotated pair's own entry G'[cP][cQ] keeps its rounding
+                // residue: the pair is not met again in this visit.)
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    const int r = warp + 8 * h;
+                    cf x = H[gidx(r, cP)], y = H[gidx(r, cQ)];
+                    rotate_cols(x, y, tp, sg);
+                    gP[h] = x;
+                    gQ[h] = y;
+                    rotate_cols(eP[h], eQ[h], tp, sg);
+                    const float mp = r == cP ? 1.f : 0.f, mq = r == cQ ? 1.f : 0.f;
+                    eP[h].x = fmaf(-mp, tp, fmaf(-mq, sg.x, eP[h].x));
+                    eP[h].y = fmaf(-mq, sg.y, eP[h].y);
+                    eQ[h].x = fmaf(mp, sg.x, fmaf(-mq, tp, eQ[h].x));
+                    eQ[h].y = fmaf(-mp, sg.y, eQ[h].y);
+                }
+            }
+            if (s + 1 < nsteps) {
+                // the columns move to the lanes of the next step's pairs
+                if (!full) {
+                    const int src = (lane + 1) & 31;
+#pragma unroll
+                    for (int h = 0; h < 8; ++h) {
+                        gQ[h] = shfl_cf(gQ[h], src);
+                        eQ[h] = shfl_cf(eQ[h], src);
+                    }
+                    cQ = __shfl_sync(0xffffffffu, cQ, src);
+                } else {
+#pragma unroll
+                    for (int h = 0; h < 8; ++h) {
+                        circle_move(gP[h], gQ[h], lane);
+                        circle_move(eP[h], eQ[h], lane);
+                    }
+                    circle_move_idx(cP, cQ, lane);
+                }
+                publish_gamma(gQ, warp, cP, ax.gam + lane);
+            }
+            __syncthreads();
+        }
+        // E (row-major) for the update's B operand
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
             const int r = warp + 8 * h;
-            cf x = H[gidx(r, p)], y = H[gidx(r, q)];
-            if (rot) rotate_cols(x, y, tp, sg);
-            if (r == p) {                 // (p, p) and (p, q)
-                x.y = 0.f;
-                if (rot) y = cmake(0.f, 0.f);
-                ax.diag[p] = x.x;
-            } else if (r == q) {          // (q, p) and (q, q)
-                y.y = 0.f;
-                if (rot) x = cmake(0.f, 0.f);
-                ax.diag[q] = y.x;
-            }
-            G[gidx(r, p)] = x;
-            G[gidx(r, q)] = y;
-            if (rot) {
-                const cf ex = E[r * TJ_W + p], ey = E[r * TJ_W + q];
-                cf ux = cmake(ex.x + (r == p ? 1.f : 0.f), ex.y);
-                cf uy = cmake(ey.x + (r == q ? 1.f : 0.f), ey.y);
-                E[r * TJ_W + p] = csub(ex, cadd(cscale(ux, tp), cmul(uy, sg)));
-                E[r * TJ_W + q] = cadd(ey, csub(cmul(ux, cconj(sg)), cscale(uy, tp)));
-            }
+            E[r * TJ_W + cP] = eP[h];
+            E[r * TJ_W + cQ] = eQ[h];
         }
-        __syncthreads();
     }
     const long long c2 = clock64();
     const bool rotated = work && rsteps > 0;
@@ -448,101 +542,87 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
     if (rotated && tid == 0) atomicMax(reinterpret_cast<int*>(g.offmax + j), __float_as_int(ax.cmax));
 
     // ---- 3. Y <- Y + Y E ---------------------------------------------------
+    // Real form without the -i Y rows: D1 = Y Re E and D2 = Y Im E (M = the
+    // 128 interleaved reals of 64 rows, N = 128: Re E's columns then Im E's,
+    // K = the 64 visit columns), then Re y' = Re y + D1(re) - D2(im) and
+    // Im y' = Im y + D2(re) + D1(im): the two reals of a row are adjacent
+    // TMEM lanes, one shuffle apart.  All three pieces of a chunk's A tile fit
+    // beside B, so one step (24 MMAs) per 64 rows; the chunk's pieces arrive
+    // by cp.async while the previous chunk's epilogue runs.
     if (rotated) {
-        uint4 pv[4];
-        load_rot_piece(pv, P, pplane, ax.col, lslot, 0, 2, tid);   // overlaps the B build
         __syncthreads();                                   // the diagonal above is read
-        // B pieces at [0, 48K): element (q, k) of piece i at i*16K + (k/64)*8K
-        // + sw128_off(q, k % 64); k < 64: Re E[k][q], k >= 64: -Im E[k-64][q].
-        // Task (q, k-group of 8): 64 x 16 = 1024 tasks, 4 a thread.
+        // B pieces at [0, 48K): row n of piece i at i*16K + sw128_off(n, k),
+        // k = the visit column; n < 64: Re E[k][n], n >= 64: Im E[k][n-64].
+        // Task (n, k-group of 8): 128 x 8 = 1024 tasks, 4 a thread.
 #pragma unroll 1
         for (int h = 0; h < 4; ++h) {
             const int task = tid + TJ_T * h;
-            const int q = task & 63, kg = task >> 6;       // kg in 0..15
+            const int n = task & 127, kg = task >> 7;      // kg in 0..7
             float v[8];
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-                const int k = kg * 8 + e;
-                const cf x = E[(k & 63) * TJ_W + q];
-                v[e] = k < 64 ? x.x : -x.y;
+                const cf x = E[(kg * 8 + e) * TJ_W + (n & 63)];
+                v[e] = n < 64 ? x.x : x.y;
             }
-            put_pieces(smem, TJ_PIECE, (uint32_t)(kg >> 3) * 8192u + tc::sw128_off(q, (kg & 7) * 8), v);
+            put_pieces(smem, TJ_PIECE, tc::sw128_off(n, kg * 8), v);
         }
         __syncthreads();                                   // E is dead
-        uint8_t* At = smem + TJ_AOFF;
-        constexpr uint32_t IDESC_R = tc::idesc_bf16(128, 64, true, false);
+        uint8_t* At = smem + TJ_AOFF;                      // piece i at At + i*16K
+        constexpr uint32_t IDESC_U = tc::idesc_bf16(128, 128, true, false);
         const int npair = lslot / 64;
-        // the epilogue's elements: real mreal of the chunk, columns q0..q0+31
-        const int mreal = 32 * (warp & 3) + lane;
+        const int mreal = 32 * (warp & 3) + lane;          // TMEM lane: real of the chunk
         const int q0 = 32 * (warp >> 2);
-        const uint8_t* xsrc = At + (uint32_t)(mreal >> 6) * TJ_PIECE;
-        // Y of the epilogue's elements, summed from the pieces as they pass
-        // through the tile, is parked in TMEM columns 64..127 (the MMAs use
-        // 0..63) between the steps
-        const uint32_t tpark = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 64u + (uint32_t)q0;
-        for (int cp = 0; ok && cp < npair; ++cp) {
-            // piece products smallest first: A2 B0 | A1 B1, A1 B0 | A0 B2,
-            // A0 B1, A0 B0, each over all eight K steps
-            for (int step = 0; step < 3; ++step) {
-                const int ia = 2 - step;
+        const uint32_t xoff = (uint32_t)(mreal >> 6) * TJ_MGRP;
+        const bool re_lane = (mreal & 1) == 0;
+        load_update_pieces(At, P, pplane, ax.col, lslot, 0, tid);
+        for (int cp = 0; cp < npair; ++cp) {
+            tc::cp_async_wait_all();
+            tc::fence_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint32_t sa = tc::smem_u32(At), sb = tc::smem_u32(smem);
+                // piece products smallest first: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)
+                const int pa[6] = {2, 1, 0, 1, 0, 0};
+                const int pb[6] = {0, 1, 2, 0, 1, 0};
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    const int t = tid + TJ_T * h;
-                    const int p = t >> 4, gg = t & 15;
-                    const uint32_t mo = (uint32_t)(gg >> 3) * TJ_PIECE;
-                    *reinterpret_cast<uint4*>(At + mo + tc::sw128_off(p, (gg & 7) * 8)) = pv[h];
-                    *reinterpret_cast<uint4*>(At + mo + tc::sw128_off(TJ_W + p, (gg & 7) * 8)) =
-                        twist_packed(pv[h]);
-                }
-                tc::fence_async_smem();
-                __syncthreads();
-                if (tid == 0) {
-                    tc::fence_after_sync();
-                    const uint32_t sa = tc::smem_u32(At), sb = tc::smem_u32(smem);
-                    for (int ib = 2 - ia; ib >= 0; --ib)
-#pragma unroll 1
-                        for (int ks = 0; ks < 8; ++ks)
-                            tc::mma_bf16(tmem, tc::sdesc(sa + ks * 2048, TJ_PIECE, 1024),
-                                         tc::sdesc(sb + ib * TJ_PIECE + (ks >> 2) * 8192 +
-                                                       (ks & 3) * 32, 16, 1024),
-                                         IDESC_R, (step | ks | (ib != 2 - ia)) != 0);
-                    tc::mma_commit(&ax.bar[0]);
-                }
-                // this piece of the epilogue's elements, from the tile (the
-                // sum p2 + p1 + p0 is exact in any order of these steps)
-                {
-                    float xacc[32];
-                    if (step > 0) tc::tmem_ld32(tpark, xacc);
+                for (int q = 0; q < 6; ++q)
 #pragma unroll
-                    for (int e = 0; e < 32; ++e) {
-                        const float x = bf16_bits(*reinterpret_cast<const uint16_t*>(
-                            xsrc + tc::sw128_off(q0 + e, mreal & 63)));
-                        xacc[e] = step == 0 ? x : xacc[e] + x;
-                    }
-                    tc::tmem_st32(tpark, xacc);
-                }
-                // the next piece's loads overlap the MMAs
-                if (step < 2)
-                    load_rot_piece(pv, P, pplane, ax.col, lslot, cp, ia - 1, tid);
-                else if (cp + 1 < npair)
-                    load_rot_piece(pv, P, pplane, ax.col, lslot, cp + 1, 2, tid);
-                ok = __syncthreads_and(wait_mma(&ax.bar[0], ph0)) != 0;
-                if (!ok) break;
+                    for (int ks = 0; ks < 4; ++ks)
+                        tc::mma_bf16(tmem, tc::sdesc(sa + pa[q] * TJ_PIECE + ks * 2048, TJ_MGRP, 1024),
+                                     tc::sdesc(sb + pb[q] * TJ_PIECE + ks * 32, 16, 1024), IDESC_U,
+                                     (q | ks) != 0);
+                tc::mma_commit(&ax.bar[0]);
             }
+            // Y of this thread's elements (real mreal, columns q0..q0+31),
+            // summed from the three pieces in the tile (exact)
+            float xr[32];
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+                const uint32_t o = xoff + tc::sw128_off(q0 + e, mreal & 63);
+                xr[e] = bf16_bits(*reinterpret_cast<const uint16_t*>(At + o)) +
+                        (bf16_bits(*reinterpret_cast<const uint16_t*>(At + TJ_PIECE + o)) +
+                         bf16_bits(*reinterpret_cast<const uint16_t*>(At + 2 * TJ_PIECE + o)));
+            }
+            ok = __syncthreads_and(wait_mma(&ax.bar[0], ph0)) != 0;
             if (!ok) break;
             tc::fence_after_sync();
-            // epilogue: Y + D in FP32 with round-to-nearest, then its pieces
+            // the tile is free: the next chunk's pieces load during the epilogue
+            if (cp + 1 < npair) load_update_pieces(At, P, pplane, ax.col, lslot, cp + 1, tid);
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
-                float v[16], xacc[16];
-                tc::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + q0 + 16 * half, v);
-                tc::tmem_ld16(tpark + 16 * half, xacc);
+                float d1[16], d2[16];
+                const uint32_t tl = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + q0 + 16 * half;
+                tc::tmem_ld16(tl, d1);
+                tc::tmem_ld16(tl + 64, d2);
 #pragma unroll
                 for (int e = 0; e < 16; ++e) {
+                    const float d2p = __shfl_xor_sync(0xffffffffu, d2[e], 1);
                     const int col = ax.col[q0 + 16 * half + e];
                     if (col >= 0) {
+                        const float d = re_lane ? d1[e] - d2p : d2p + d1[e];
                         const size_t off = (size_t)col * 2 * lslot + (size_t)cp * 128 + mreal;
-                        const tc::Split3 sp = tc::split3(xacc[e] + v[e]);
+                        const tc::Split3 sp = tc::split3(xr[16 * half + e] + d);
                         P[off] = __bfloat16_as_ushort(sp.p0);
                         P[pplane + off] = __bfloat16_as_ushort(sp.p1);
                         P[2 * pplane + off] = __bfloat16_as_ushort(sp.p2);
@@ -550,9 +630,8 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                 }
             }
             tc::fence_before_sync();
-            __syncthreads();
-            tc::fence_after_sync();
         }
+        __syncthreads();
     }
     if (tid == 0) {
         const long long c3 = clock64();
@@ -835,10 +914,10 @@ int tc_sweep_launch(const mps_2q_job* jobs, int njobs, int rounds, int pairs, co
 // Counters of the tensor-core visits (g_tj_cycles), reset after reading when
 // reset != 0.  Blocks.
 extern "C" int mps_tc_profile(unsigned long long* out10, int reset) {
-    unsigned long long v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long v[10] = {0};
     MPS_CUDA_CHECK(cudaMemcpyFromSymbol(v, mps::g_tj_cycles, sizeof(v)));
     if (reset) {
-        const unsigned long long z[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const unsigned long long z[10] = {0};
         MPS_CUDA_CHECK(cudaMemcpyToSymbol(mps::g_tj_cycles, z, sizeof(z)));
     }
     if (out10)
