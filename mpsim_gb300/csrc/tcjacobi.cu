@@ -198,8 +198,24 @@ __device__ __forceinline__ uint4 twist_packed(uint4 w) {
     return w;
 }
 
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
-    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+// Two reals -> their three bf16 pieces, packed in pairs (a in the low half),
+// with the paired round-to-nearest conversion: the same pieces as
+// tc::split3, in three conversions instead of six.
+struct Pieces2 {
+    uint32_t w0, w1, w2;
+};
+__device__ __forceinline__ Pieces2 split3x2(float a, float b) {
+    const __nv_bfloat162 p0 = __floats2bfloat162_rn(a, b);
+    const float2 f0 = __bfloat1622float2(p0);
+    const float ra = a - f0.x, rb = b - f0.y;            // exact
+    const __nv_bfloat162 p1 = __floats2bfloat162_rn(ra, rb);
+    const float2 f1 = __bfloat1622float2(p1);
+    const __nv_bfloat162 p2 = __floats2bfloat162_rn(ra - f1.x, rb - f1.y);
+    Pieces2 r;
+    r.w0 = *reinterpret_cast<const uint32_t*>(&p0);
+    r.w1 = *reinterpret_cast<const uint32_t*>(&p1);
+    r.w2 = *reinterpret_cast<const uint32_t*>(&p2);
+    return r;
 }
 
 // 8 reals -> the 16-byte chunks of all three pieces, in buffers `stride`
@@ -209,10 +225,10 @@ __device__ __forceinline__ void put_pieces(uint8_t* base, size_t stride, uint32_
     uint32_t w[3][4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-        const tc::Split3 a = tc::split3(v[2 * e]), b = tc::split3(v[2 * e + 1]);
-        w[0][e] = pack2(a.p0, b.p0);
-        w[1][e] = pack2(a.p1, b.p1);
-        w[2][e] = pack2(a.p2, b.p2);
+        const Pieces2 q = split3x2(v[2 * e], v[2 * e + 1]);
+        w[0][e] = q.w0;
+        w[1][e] = q.w1;
+        w[2][e] = q.w2;
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -224,30 +240,31 @@ __device__ __forceinline__ float bf16_bits(uint16_t u) {
     return __uint_as_float((uint32_t)u << 16);
 }
 
-// Gram task t (0..1535) = (column p, piece i, 16-byte chunk g of the 128
-// bytes a piece column holds for 32 rows).
-__device__ __forceinline__ void gram_task(int t, int& p, int& i, int& g) {
-    p = t / 24;
-    const int rem = t - 24 * p;
-    i = rem >> 3;
-    g = rem & 7;
-}
-
-// Step-1 loads of rows 32c..32c+31: 1536 tasks, 6 a thread.
-__device__ __forceinline__ void load_gram_pieces(uint4 (&v)[6], const uint16_t* P, size_t pplane,
-                                                 const int* col, int lslot, int c, int tid) {
+// The Gram's per-thread tasks, fixed for a visit: task t = tid + 256 h
+// (0..1535) = (column p, piece i, 16-byte chunk g of the 128 bytes a piece
+// column holds for 32 rows).  soff: its Y row's offset in a tile buffer (the
+// T row is 8 KB further: rows 64 + p share p's swizzle); goff: its source in
+// the planes, less the chunk's 64 c (~0u: a padding column).
+__device__ __forceinline__ void gram_tasks(uint32_t (&soff)[6], uint32_t (&goff)[6],
+                                           const int* col, int lslot, size_t pplane, int tid) {
 #pragma unroll
     for (int h = 0; h < 6; ++h) {
-        int p, i, g;
-        gram_task(tid + TJ_T * h, p, i, g);
+        const int t = tid + TJ_T * h;
+        const int p = t / 24, rem = t - 24 * (t / 24);
+        const int i = rem >> 3, g = rem & 7;
+        soff[h] = (uint32_t)i * TJ_PIECE + tc::sw128_off(p, g * 8);
         const int cc = col[p];
-        if (cc >= 0) {
-            const uint16_t* src = P + i * pplane + (size_t)cc * 2 * lslot + (size_t)c * 64 + g * 8;
-            v[h] = __ldcg(reinterpret_cast<const uint4*>(src));
-        } else {
-            v[h] = make_uint4(0u, 0u, 0u, 0u);
-        }
+        goff[h] = cc >= 0 ? (uint32_t)((size_t)i * pplane + (size_t)cc * 2 * lslot + g * 8) : ~0u;
     }
+}
+
+// Step-1 loads of rows 32c..32c+31: 6 16-byte chunks a thread.
+__device__ __forceinline__ void load_gram_pieces(uint4 (&v)[6], const uint16_t* P,
+                                                 const uint32_t (&goff)[6], int c) {
+#pragma unroll
+    for (int h = 0; h < 6; ++h)
+        v[h] = goff[h] != ~0u ? __ldcg(reinterpret_cast<const uint4*>(P + goff[h] + (size_t)c * 64))
+                              : make_uint4(0u, 0u, 0u, 0u);
 }
 
 // Step-3 loads of rows 64cp..64cp+63 (128 reals, 256 bytes a piece column)
@@ -310,8 +327,10 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
         float acc[32];
 #pragma unroll
         for (int e = 0; e < 32; ++e) acc[e] = 0.f;
+        uint32_t soff[6], goff[6];
+        gram_tasks(soff, goff, ax.col, lslot, pplane, tid);
         uint4 pre[6];
-        load_gram_pieces(pre, P, pplane, ax.col, lslot, 0, tid);
+        load_gram_pieces(pre, P, goff, 0);
         int waited = -1;                  // chunks <= waited are summed into acc
         for (int c = 0; c < nchunk; ++c) {
             const int b = c & 1;
@@ -327,12 +346,12 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             uint8_t* tile = smem + b * TJ_GTILE;
 #pragma unroll
             for (int h = 0; h < 6; ++h) {
-                int p, i, gg;
-                gram_task(tid + TJ_T * h, p, i, gg);
-                uint8_t* t = tile + i * TJ_PIECE;
-                *reinterpret_cast<uint4*>(t + tc::sw128_off(p, gg * 8)) = pre[h];
-                *reinterpret_cast<uint4*>(t + tc::sw128_off(TJ_W + p, gg * 8)) = twist_packed(pre[h]);
+                *reinterpret_cast<uint4*>(tile + soff[h]) = pre[h];
+                *reinterpret_cast<uint4*>(tile + soff[h] + TJ_W * 128) = twist_packed(pre[h]);
             }
+            // the next chunk's loads overlap this chunk's MMAs and the next
+            // accumulator read
+            if (c + 1 < nchunk) load_gram_pieces(pre, P, goff, c + 1);
             tc::fence_async_smem();
             __syncthreads();
             if (tid == 0) {
@@ -351,7 +370,6 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                                      (ks | q) != 0);
                 tc::mma_commit(&ax.bar[b]);
             }
-            if (c + 1 < nchunk) load_gram_pieces(pre, P, pplane, ax.col, lslot, c + 1, tid);
         }
         // the last one or two chunks (every phase is waited on, so the
         // barriers' parities stay in step)
@@ -609,23 +627,35 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             tc::fence_after_sync();
             // the tile is free: the next chunk's pieces load during the epilogue
             if (cp + 1 < npair) load_update_pieces(At, P, pplane, ax.col, lslot, cp + 1, tid);
+            // Per 16 columns: y of this lane's real, then the two lanes of a
+            // row swap halves so that each holds (re, im) of 8 columns and
+            // writes one 4-byte word per piece plane and column.
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
                 float d1[16], d2[16];
                 const uint32_t tl = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + q0 + 16 * half;
                 tc::tmem_ld16(tl, d1);
                 tc::tmem_ld16(tl + 64, d2);
+                float y[16];
 #pragma unroll
                 for (int e = 0; e < 16; ++e) {
                     const float d2p = __shfl_xor_sync(0xffffffffu, d2[e], 1);
-                    const int col = ax.col[q0 + 16 * half + e];
+                    y[e] = xr[16 * half + e] + (re_lane ? d1[e] - d2p : d2p + d1[e]);
+                }
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    // even lane: columns e (its re, the partner's im); odd
+                    // lane: columns 8 + e (the partner's re, its im)
+                    const float send = re_lane ? y[8 + e] : y[e];
+                    const float got = __shfl_xor_sync(0xffffffffu, send, 1);
+                    const float vr = re_lane ? y[e] : got, vi = re_lane ? got : y[8 + e];
+                    const int col = ax.col[q0 + 16 * half + (re_lane ? e : 8 + e)];
                     if (col >= 0) {
-                        const float d = re_lane ? d1[e] - d2p : d2p + d1[e];
-                        const size_t off = (size_t)col * 2 * lslot + (size_t)cp * 128 + mreal;
-                        const tc::Split3 sp = tc::split3(xr[16 * half + e] + d);
-                        P[off] = __bfloat16_as_ushort(sp.p0);
-                        P[pplane + off] = __bfloat16_as_ushort(sp.p1);
-                        P[2 * pplane + off] = __bfloat16_as_ushort(sp.p2);
+                        const size_t off = (size_t)col * 2 * lslot + (size_t)cp * 128 + (mreal & ~1);
+                        const Pieces2 q = split3x2(vr, vi);
+                        *reinterpret_cast<uint32_t*>(P + off) = q.w0;
+                        *reinterpret_cast<uint32_t*>(P + pplane + off) = q.w1;
+                        *reinterpret_cast<uint32_t*>(P + 2 * pplane + off) = q.w2;
                     }
                 }
             }
