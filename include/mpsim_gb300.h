@@ -94,9 +94,8 @@ typedef struct {
  *   operands (every FP32 value split into three bf16 pieces, six piece
  *   products accumulated in FP32 in TMEM: FP32-grade products); the rotation
  *   parameters come from G in shared memory, the off-diagonal test is FP64.
- *   Every job of the call must be tall (m >= n) and left-canonical with at
- *   least 64 columns (MPS_ERR_ARG otherwise); mpsim_gb300's Python layer
- *   routes other jobs to a PLAIN call. */
+ *   This form covers the tall (m >= n), left-canonical jobs of 64+ columns;
+ *   the call's other jobs take the PLAIN sweeps in the same sweep loop. */
 #define MPS_PRECISION_PLAIN 0
 #define MPS_PRECISION_MIXED 1
 

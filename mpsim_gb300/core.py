@@ -950,45 +950,28 @@ class MPS:
             self._norms.append(self.norm())
 
     def _run_pairs(self, pairs):
-        """One batched launch for two-qudit gates on disjoint adjacent pairs
-        (two with precision="mixed": the gates the tensor-core sweeps take,
-        and the rest)."""
+        """One batched launch for two-qudit gates on disjoint adjacent pairs.
+        With precision="mixed" the call is MPS_PRECISION_MIXED: the gates the
+        tensor-core sweeps take (left-canonical, tall, 64+ columns) run
+        there, the rest in the SIMT sweeps of the same call; "auto" does so
+        when the tuning table measured the mixed form faster for the
+        tensor-core gates' shape and count."""
         if not pairs:
             return
+        precision = _native.PRECISION_PLAIN
         if self.precision in ("mixed", "auto"):
             d = self._qudit_dimension
-            tc, rest, tags_tc, tags_rest = [], [], [], []
-            for q, p in enumerate(pairs):
-                chil = int(self._site_list[p[1]].shape[0])
-                chir = int(self._site_list[p[1] + 1].shape[2])
-                m, n = chil * d, chir * d
+            tc = []
+            for p in pairs:
+                m = int(self._site_list[p[1]].shape[0]) * d
+                n = int(self._site_list[p[1] + 1].shape[2]) * d
                 if p[3] and m >= n and n >= 64:
-                    tc.append(p)
-                    tags_tc.append(q)
-                else:
-                    rest.append(p)
-                    tags_rest.append(q)
-            h0 = len(self.svals_history)
-            if tc and self.precision == "auto":
-                mm = max(int(self._site_list[p[1]].shape[0]) * d for p in tc)
-                nn = max(int(self._site_list[p[1] + 1].shape[2]) * d for p in tc)
-                if autotune.lookup(mm, nn, d, len(tc))["precision"] != "mixed":
-                    rest, tags_rest = tc + rest, tags_tc + tags_rest
-                    tc, tags_tc = [], []
-            if tc:
-                self._run_pair_group(tc, _native.PRECISION_MIXED)
-            if rest:
-                self._run_pair_group(rest, _native.PRECISION_PLAIN)
-            if self.record_svals and tc and rest:
-                # keep the history in the order the gates were given
-                new = self.svals_history[h0:]
-                tags = tags_tc + tags_rest
-                ordered = [None] * len(tags)
-                for pos, q in enumerate(tags):
-                    ordered[q] = new[pos]
-                self.svals_history[h0:] = ordered
-        else:
-            self._run_pair_group(pairs, _native.PRECISION_PLAIN)
+                    tc.append((m, n))
+            if tc and (self.precision == "mixed" or autotune.lookup(
+                    max(m for m, _ in tc), max(n for _, n in tc), d,
+                    len(tc))["precision"] == "mixed"):
+                precision = _native.PRECISION_MIXED
+        self._run_pair_group(pairs, precision)
 
     def _run_pair_group(self, pairs, precision):
         """One mps_apply_2q_batch call for gates on disjoint adjacent pairs."""

@@ -583,7 +583,8 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
         if (active) {
             const JobShape sh = job_shape<BC>(jobs, j, g.d);
             nb = sh.nb;
-            active = sh.C >= 2 && r < sh.nb - 1 && p < sh.nb / 2;
+            active = sh.C >= 2 && r < sh.nb - 1 && p < sh.nb / 2 &&
+                     !(g.tc_mode && tc_job(sh.m, sh.n, jobs[j].keep_left_canonical));
             if (active) tournament_pair(sh.nb, r, p, I, J);
         }
         if (active) {
@@ -735,6 +736,7 @@ presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2, int b
             __syncthreads();
         }
     }
+    if (g.tc_mode && tc_job(m, n, jobs[j].keep_left_canonical)) bc = 32;   // tensor-core blocks
     if (g.vstamp) {
         // a block whose set of columns changes counts as changed (its pairs
         // are not the ones last checked); moves inside a block do not
@@ -1500,8 +1502,12 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         return fail(MPS_ERR_ARG, "mps_apply_2q_batch: block_request must be 0, 8 or 16");
     sweep_fn sweep = pick_sweep(lw, block_request);
     if (block_request == 8 && lw > 256 && lw <= 576) bc = 8;
-    if (mixed) bc = 32;
-    if (params) params->block_cols = bc;
+    // MPS_PRECISION_MIXED: the left-canonical tall jobs of 64+ columns take
+    // the tensor-core sweeps (32-column blocks), the others the SIMT ones, in
+    // the same sweep loop
+    g.tc_mode = mixed ? 1 : 0;
+    constexpr int kTcBlock = 32;
+    if (params) params->block_cols = mixed ? kTcBlock : bc;
     SweepSync sync;
     sync.next_item = reinterpret_cast<int*>(ws + lo.off_sync);
     sync.error = sync.next_item + 1;
@@ -1509,9 +1515,6 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     sync.nbmax = lo.nbmax;
     sync.wait_limit = (params && params->wait_limit > 0) ? params->wait_limit : (1 << 22);
     sync.stall_test = params ? params->stall_test : 0;
-    if (mixed && (lo.lslot % 64 != 0 || min(max_m, max_n) < 64))
-        return fail(MPS_ERR_ARG, "mps_apply_2q_batch: MPS_PRECISION_MIXED needs jobs of 64+ "
-                                 "columns");
     // padding rows and columns of X must be zero; no block has a stamp yet
     MPS_CUDA_CHECK(cudaMemsetAsync(g.X, 0, lo.off_V - lo.off_X, s));
     MPS_CUDA_CHECK(cudaMemsetAsync(g.vstamp, 0xff, lo.off_qst - lo.off_vst +
@@ -1532,10 +1535,17 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (rc) return rc;
 
     const int cmax = min(max_m, max_n);
-    int nbmax = (cmax + bc - 1) / bc;
-    if (nbmax < 2) nbmax = 2;
-    nbmax += nbmax & 1;
+    auto block_count = [&](int width) {
+        int nb = (cmax + width - 1) / width;
+        if (nb < 2) nb = 2;
+        return nb + (nb & 1);
+    };
+    const int nbmax = block_count(bc);
     const int rounds = nbmax - 1, pairs = nbmax / 2;
+    const int nb_tc = block_count(kTcBlock);
+    const int rounds_tc = nb_tc - 1, pairs_tc = nb_tc / 2;
+    // stamps of every sweep lie above those of the sweeps before it
+    const int tbase_stride = rounds + 1;
 
     if (!t_pinned && !capturing) {
         MPS_CUDA_CHECK(cudaHostAlloc(reinterpret_cast<void**>(&t_pinned), 8 * sizeof(int),
@@ -1549,40 +1559,37 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     if (cmax >= 2) {
         for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
             MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
+            if (cmax > 2 * bc) {
+                presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc,
+                                                                   sweeps * tbase_stride);
+                MPS_LAUNCH_CHECK("presort_kernel");
+            }
+            MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
+                                           (size_t)njobs * lo.nbmax * sizeof(int), s));
             if (mixed) {
-                // tensor-core block sweeps, one persistent launch per sweep
-                // with the same round flags and visit stamps as the SIMT
-                // form; X is split into its bf16 pieces once, before the
-                // first sweep (an expired wait stays in sync.error until the
-                // call returns)
+                // the tensor-core jobs: one persistent launch per sweep with
+                // the same round flags and visit stamps as the SIMT form (its
+                // own item counter, counter[2]); X is split into its bf16
+                // pieces before the first sweep.  An expired wait stays in
+                // sync.error until the call returns.
                 if (sweeps == 1) {
                     MPS_CUDA_CHECK(cudaMemsetAsync(sync.error, 0, sizeof(int), s));
-                    if (int e = tc_split_launch(njobs, g, s)) return e;
+                    if (int e = tc_split_launch(jobs, njobs, g, s)) return e;
                 }
-                if (cmax > 2 * bc) {
-                    presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc,
-                                                                       sweeps * (rounds + 1));
-                    MPS_LAUNCH_CHECK("presort_kernel");
-                }
+                SweepSync tsync = sync;
+                tsync.next_item = g.counter + 2;
+                MPS_CUDA_CHECK(cudaMemsetAsync(tsync.next_item, 0, sizeof(int), s));
+                rc = tc_sweep_launch(jobs, njobs, rounds_tc, pairs_tc, g, tol2, tsync,
+                                     sweeps * tbase_stride, s);
+                if (rc) return rc;
                 MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, sizeof(int), s));
-                MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
-                                               (size_t)njobs * lo.nbmax * sizeof(int), s));
-                rc = tc_sweep_launch(jobs, njobs, rounds, pairs, g, tol2, sync,
-                                     sweeps * (rounds + 1), s);
-                if (rc) return rc;
             } else {
-                if (cmax > 2 * bc) {
-                    presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc,
-                                                                       sweeps * (rounds + 1));
-                    MPS_LAUNCH_CHECK("presort_kernel");
-                }
-                // one persistent launch runs every round of the sweep
                 MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, 2 * sizeof(int), s));
-                MPS_CUDA_CHECK(cudaMemsetAsync(sync.block_round, 0xff,
-                                               (size_t)njobs * lo.nbmax * sizeof(int), s));
-                rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, sweeps * (rounds + 1), s);
-                if (rc) return rc;
             }
+            // the SIMT jobs (all of them in the plain form): one persistent
+            // launch runs every round of the sweep
+            rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, sweeps * tbase_stride, s);
+            if (rc) return rc;
             sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2, sync.error);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
             if (capturing) {
@@ -1592,7 +1599,7 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
             MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, 2 * sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
             if (mixed)
-                MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 3, g.counter + 2, 2 * sizeof(int),
+                MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 4, g.counter + 3, sizeof(int),
                                                cudaMemcpyDeviceToHost, s));
             MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 2, sync.error, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
@@ -1600,14 +1607,9 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
             if (t_pinned[2] != 0)
                 return fail(MPS_ERR_TIMEOUT, "mps_apply_2q_batch: a round-dependency wait inside the "
                                              "sweep kernel expired; results are invalid");
-            if (mixed) {
-                if (t_pinned[3] != 0)
-                    return fail(MPS_ERR_ARG, "mps_apply_2q_batch: MPS_PRECISION_MIXED takes only "
-                                             "left-canonical tall jobs of 64+ columns");
-                if (t_pinned[4] != 0)
-                    return fail(MPS_ERR_TIMEOUT, "mps_apply_2q_batch: a tensor-core MMA wait "
-                                                 "expired; results are invalid");
-            }
+            if (mixed && t_pinned[4] != 0)
+                return fail(MPS_ERR_TIMEOUT, "mps_apply_2q_batch: a tensor-core MMA wait "
+                                             "expired; results are invalid");
             if (t_pinned[0] == 0) {
                 converged = true;
                 break;
@@ -1615,8 +1617,8 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         }
         if (sweeps > max_sweeps) sweeps = max_sweeps;
         if (mixed) {
-            // the tensor-core sweeps kept the columns in the piece planes
-            rc = tc_merge_launch(njobs, g, s);
+            // the tensor-core sweeps kept their jobs' columns in the piece planes
+            rc = tc_merge_launch(jobs, njobs, g, s);
             if (rc) return rc;
         }
     } else {
@@ -1764,6 +1766,7 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
     g.qstride = lo.qstride;
     g.P = nullptr;
     g.pplane = 0;
+    g.tc_mode = 0;
 
     int max_sweeps = 40;
     float tol = 0.f;

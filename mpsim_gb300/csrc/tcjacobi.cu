@@ -164,6 +164,11 @@ __device__ __forceinline__ void circle_move(cf& t, cf& b, int lane) {
     t = nt;
     b = nb;
 }
+// (top, bottom) of one lane packed as (x, y).
+__device__ __forceinline__ void circle_move_pair(cf& tb, int lane) {
+    const float nt = circle_top(tb.x, tb.y, lane), nb = circle_bottom(tb.x, tb.y, lane);
+    tb = cmake(nt, nb);
+}
 __device__ __forceinline__ void circle_move_idx(int& t, int& b, int lane) {
     const int up = __shfl_up_sync(0xffffffffu, t, 1);
     const int b0 = __shfl_sync(0xffffffffu, b, 0);
@@ -455,6 +460,8 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             eQ[h] = cmake(0.f, 0.f);
         }
         publish_gamma(gQ, warp, cP, ax.gam + lane);
+        // the diagonal of this lane's columns, kept in every warp alike
+        float dP = ax.diag[cP], dQ = ax.diag[cQ];
         __syncthreads();
         for (int s = 0; s < nsteps; ++s) {
             // this warp's copy of the step's 32 rotations: lane k holds pair k
@@ -464,7 +471,7 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             cf sg = cmake(0.f, 0.f);
             bool rot;
             {
-                const float a = ax.diag[cP], b = ax.diag[cQ];
+                const float a = dP, b = dQ;
                 const cf gam = ax.gam[lane];
                 // per-step rotation decision in FP32 (the SIMT form's test)
                 rot = pair_cos2(gam, cabs2(gam), a, b) > tol2;
@@ -491,10 +498,9 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                     H[gidx(cQ, r)] = cconj(gQ[h]);
                 }
                 __syncthreads();
-                // every warp has read this step's diagonal
-                if (warp == 0 && rot) {
-                    ax.diag[cP] = na;
-                    ax.diag[cQ] = nb;
+                if (rot) {
+                    dP = na;
+                    dQ = nb;
                 }
                 // pass 2: G' = H^H R (= R^H G R) and E <- (I + E) R - I =
                 // E R + (R - I), whose identity part adds -tp, -sigma to
@@ -526,6 +532,7 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                         eQ[h] = shfl_cf(eQ[h], src);
                     }
                     cQ = __shfl_sync(0xffffffffu, cQ, src);
+                    dQ = __shfl_sync(0xffffffffu, dQ, src);
                 } else {
 #pragma unroll
                     for (int h = 0; h < 8; ++h) {
@@ -533,11 +540,20 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                         circle_move(eP[h], eQ[h], lane);
                     }
                     circle_move_idx(cP, cQ, lane);
+                    cf d = cmake(dP, dQ);
+                    circle_move_pair(d, lane);
+                    dP = d.x;
+                    dQ = d.y;
                 }
                 publish_gamma(gQ, warp, cP, ax.gam + lane);
             }
             __syncthreads();
         }
+        if (warp == 0) {
+            ax.diag[cP] = dP;
+            ax.diag[cQ] = dQ;
+        }
+        __syncthreads();                  // the diagonal is read below
         // E (row-major) for the update's B operand
 #pragma unroll
         for (int h = 0; h < 8; ++h) {
@@ -652,10 +668,10 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                     const int col = ax.col[q0 + 16 * half + (re_lane ? e : 8 + e)];
                     if (col >= 0) {
                         const size_t off = (size_t)col * 2 * lslot + (size_t)cp * 128 + (mreal & ~1);
-                        const Pieces2 q = split3x2(vr, vi);
-                        *reinterpret_cast<uint32_t*>(P + off) = q.w0;
-                        *reinterpret_cast<uint32_t*>(P + pplane + off) = q.w1;
-                        *reinterpret_cast<uint32_t*>(P + 2 * pplane + off) = q.w2;
+                        const Pieces2 pc = split3x2(vr, vi);
+                        *reinterpret_cast<uint32_t*>(P + off) = pc.w0;
+                        *reinterpret_cast<uint32_t*>(P + pplane + off) = pc.w1;
+                        *reinterpret_cast<uint32_t*>(P + 2 * pplane + off) = pc.w2;
                     }
                 }
             }
@@ -727,10 +743,8 @@ tc_sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, double tol2d, f
             const mps_2q_job job = jobs[j];
             const int m = job.chi_l * g.d, n = job.chi_r * g.d;
             const int C = min(m, n);
-            if (job_tracks_v(m, n, job.keep_left_canonical) || C < TJ_W) {
-                // only left-canonical tall jobs of 64+ columns take these sweeps
-                if (tid == 0 && r == 0 && p == 0) atomicExch(g.counter + 2, 1);
-                active = false;
+            if (!tc_job(m, n, job.keep_left_canonical)) {
+                active = false;           // the SIMT sweep kernel's job
             } else {
                 nb = (C + TJ_BC - 1) / TJ_BC;
                 nb += nb & 1;
@@ -811,13 +825,19 @@ tc_sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, double tol2d, f
 
 // X <-> its three bf16 piece planes, every element of every job's slot, 8
 // reals a thread (a slot holds 2 lslot cslot reals, a multiple of 64).
-__global__ void __launch_bounds__(256) tc_split_kernel(TwoQGeom g, int njobs) {
+__device__ __forceinline__ bool tc_job_at(const mps_2q_job* jobs, size_t j, int d) {
+    return tc_job(jobs[j].chi_l * d, jobs[j].chi_r * d, jobs[j].keep_left_canonical);
+}
+
+__global__ void __launch_bounds__(256)
+tc_split_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int njobs) {
     const size_t per8 = g.pplane / 8;
     const size_t total8 = per8 * (size_t)njobs;
     const float4* X = reinterpret_cast<const float4*>(g.X);
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total8;
          e += (size_t)gridDim.x * blockDim.x) {
         const size_t jj = e / per8, off = (e - jj * per8) * 8;
+        if (!tc_job_at(jobs, jj, g.d)) continue;
         const float4 lo = __ldcs(X + 2 * e), hi = __ldcs(X + 2 * e + 1);
         const float v[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
         uint8_t* base = reinterpret_cast<uint8_t*>(g.P + jj * 3 * g.pplane + off);
@@ -825,13 +845,15 @@ __global__ void __launch_bounds__(256) tc_split_kernel(TwoQGeom g, int njobs) {
     }
 }
 
-__global__ void __launch_bounds__(256) tc_merge_kernel(TwoQGeom g, int njobs) {
+__global__ void __launch_bounds__(256)
+tc_merge_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int njobs) {
     const size_t per8 = g.pplane / 8;
     const size_t total8 = per8 * (size_t)njobs;
     float4* X = reinterpret_cast<float4*>(g.X);
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total8;
          e += (size_t)gridDim.x * blockDim.x) {
         const size_t jj = e / per8, off = (e - jj * per8) * 8;
+        if (!tc_job_at(jobs, jj, g.d)) continue;
         const uint16_t* base = g.P + jj * 3 * g.pplane + off;
         const uint4 w0 = __ldcs(reinterpret_cast<const uint4*>(base));
         const uint4 w1 = __ldcs(reinterpret_cast<const uint4*>(base + g.pplane));
@@ -860,18 +882,18 @@ int split_grid(const TwoQGeom& g, int njobs) {
 
 }  // namespace
 
-int tc_split_launch(int njobs, const TwoQGeom& g, cudaStream_t s) {
+int tc_split_launch(const mps_2q_job* jobs, int njobs, const TwoQGeom& g, cudaStream_t s) {
     if (!g.P) return fail(MPS_ERR_ARG, "tc sweeps: the workspace has no piece planes");
     if (g.pplane % 64 != 0) return fail(MPS_ERR_ARG, "tc sweeps: unsupported slot size");
-    tc_split_kernel<<<split_grid(g, njobs), 256, 0, s>>>(g, njobs);
+    tc_split_kernel<<<split_grid(g, njobs), 256, 0, s>>>(jobs, g, njobs);
     MPS_LAUNCH_CHECK("tc_split_kernel");
     return MPS_OK;
 }
 
-int tc_merge_launch(int njobs, const TwoQGeom& g, cudaStream_t s) {
+int tc_merge_launch(const mps_2q_job* jobs, int njobs, const TwoQGeom& g, cudaStream_t s) {
     if (!g.P) return fail(MPS_ERR_ARG, "tc sweeps: the workspace has no piece planes");
     if (g.pplane % 64 != 0) return fail(MPS_ERR_ARG, "tc sweeps: unsupported slot size");
-    tc_merge_kernel<<<split_grid(g, njobs), 256, 0, s>>>(g, njobs);
+    tc_merge_kernel<<<split_grid(g, njobs), 256, 0, s>>>(jobs, g, njobs);
     MPS_LAUNCH_CHECK("tc_merge_kernel");
     return MPS_OK;
 }

@@ -27,7 +27,8 @@ struct TwoQGeom {
     float* offmax;    // njobs: max relative off-diagonal seen this sweep
     int* done;        // njobs: 1 once a sweep made no rotation
     int* need;        // njobs: kept columns that need an orthonormal completion
-    int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf, [2] [3]: see tc_sweep_launch
+    int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf, [2] the tensor-core
+                      // sweep's item counter, [3] an expired wait (MMA or round flag)
     int* cmap;        // njobs * cslot: physical column at each sorted position
     float* cnrm;      // njobs * cslot: squared norm of each physical column
     int* scale;       // njobs: theta was multiplied by 2^scale[j] before the SVD
@@ -44,6 +45,9 @@ struct TwoQGeom {
     // tensor-core sweeps the planes, not X, hold the columns
     uint16_t* P;
     size_t pplane;
+    // 1 in MPS_PRECISION_MIXED calls: the jobs tc_job() accepts take the
+    // tensor-core sweeps, the SIMT sweep kernel the others
+    int tc_mode;
 };
 
 // Work distribution of the persistent sweep kernel.
@@ -63,6 +67,12 @@ __host__ __device__ __forceinline__ bool job_tracks_v(int m, int n, int keep_lef
     return !(m >= n && keep_left_canonical != 0);
 }
 
+// The jobs of a mixed call that take the tensor-core sweeps: left-canonical,
+// tall, 64+ columns (their left factor comes from the final columns).
+__host__ __device__ __forceinline__ bool tc_job(int m, int n, int keep_left_canonical) {
+    return !job_tracks_v(m, n, keep_left_canonical) && (m < n ? m : n) >= 64;
+}
+
 // Singular values at or below this (relative to max(s_0, 1)) are treated as
 // exact zeros: the isometric factor gets an orthonormal completion there.
 constexpr float kZeroSigma = 1e-30f;
@@ -73,16 +83,16 @@ int lq_precondition(const mps_2q_job* jobs, int njobs, int max_m, int max_n, con
                     cudaStream_t s);
 
 // Tensor-core block sweeps (tcjacobi.cu): one persistent launch runs every
-// round of one sweep of the left-canonical tall jobs, 32-column blocks, with
-// the sweep kernel's round flags (sync) and visit stamps (tbase = sweep *
-// (rounds + 1)).  counter[2] is set when a job of another kind was given,
-// counter[3] (and sync.error) when a bounded MMA wait expired.
+// round of one sweep of the tc_job() jobs, 32-column blocks, with the sweep
+// kernel's round flags (sync, with its own item counter) and visit stamps
+// (tbase).  counter[3] (and sync.error) is set when a bounded MMA wait
+// expired.
 int tc_sweep_launch(const mps_2q_job* jobs, int njobs, int rounds, int pairs, const TwoQGeom& g,
                     float tol2, const SweepSync& sync, int tbase, cudaStream_t s);
-// X -> its bf16 piece planes (before the first tensor-core sweep).
-int tc_split_launch(int njobs, const TwoQGeom& g, cudaStream_t s);
-// The piece planes summed back into X (after the last tensor-core sweep).
-int tc_merge_launch(int njobs, const TwoQGeom& g, cudaStream_t s);
+// X -> its bf16 piece planes (before the first tensor-core sweep), and the
+// planes summed back into X (after the last one), for the tc_job() jobs.
+int tc_split_launch(const mps_2q_job* jobs, int njobs, const TwoQGeom& g, cudaStream_t s);
+int tc_merge_launch(const mps_2q_job* jobs, int njobs, const TwoQGeom& g, cudaStream_t s);
 
 int merge_gate_launch(const mps_2q_job* jobs, int njobs, int max_chil, int max_chir,
                       const TwoQGeom& g, cudaStream_t s);

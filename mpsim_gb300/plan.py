@@ -17,9 +17,10 @@ of every layer is known on the host.  It then
   all of them to the device at once;
 * groups each global layer's jobs into calls: one ``mps_apply_1q_batch`` for
   every one-qudit gate of every circuit in the layer, and one
-  ``mps_apply_2q_batch`` per (precision, slot-size class) for the two-qudit
-  gates, so a few large gates do not inflate the scratch slots of many small
-  ones.  Circuits shorter than the deepest one simply drop out of the later
+  ``mps_apply_2q_batch`` per slot-size class for the two-qudit gates, so a
+  few large gates do not inflate the scratch slots of many small ones (with
+  precision="mixed" each such call is MPS_PRECISION_MIXED: its tensor-core
+  gates and its other gates share the call).  Circuits shorter than the deepest one simply drop out of the later
   layers.
 
 ``run()`` then issues only library calls -- no host work per gate, no copies
@@ -179,13 +180,11 @@ class CircuitPlan:
                     rows1.append((base + o, g1p + (gb + i) * s1, cl, cr))
             for a in range(lo, len(rows1), _CHUNK):
                 calls.append(("1q", a, min(_CHUNK, len(rows1) - a)))
-            # two-qudit gates, grouped by (precision, slot class)
+            # two-qudit gates, grouped by slot class
             groups = {}
             for ci, i, p, chil, chim, chir, k in events[t]:
                 m, n = chil * d, chir * d
-                prec = (_native.PRECISION_MIXED
-                        if precision in ("mixed", "auto") and _tc_eligible(m, n, lc)
-                        else _native.PRECISION_PLAIN)
+                elig = precision in ("mixed", "auto") and _tc_eligible(m, n, lc)
                 oa, ob = cur[ci][i][0], cur[ci][i + 1][0]
                 wa, wb = which[ci][i], which[ci][i + 1]
                 na, nbo = buf_off[ci][i][wa], buf_off[ci][i + 1][wb]
@@ -196,21 +195,23 @@ class CircuitPlan:
                        base + na if chil * k else 0, base + nbo if k * chir else 0, 0, 0,
                        status_n, chil, chim, chir, k, 1 if lc else 0, 0)
                 status_n += 1
-                groups.setdefault((prec, slot_class(m, n)), []).append((row, m, n))
-            if precision == "auto":
-                # mixed-eligible groups the tuner found faster in the plain form
-                for (prec, cls) in [g for g in groups if g[0] == _native.PRECISION_MIXED]:
-                    items = groups[(prec, cls)]
-                    mm, nn = max(x[1] for x in items), max(x[2] for x in items)
-                    if _autotune.lookup(mm, nn, d, len(items))["precision"] != "mixed":
-                        groups.setdefault((_native.PRECISION_PLAIN, cls), []).extend(
-                            groups.pop((prec, cls)))
-            for (prec, _cls), items in sorted(groups.items()):
+                groups.setdefault(slot_class(m, n), []).append((row, m, n, elig))
+            for _cls, items in sorted(groups.items()):
                 for a in range(0, len(items), _CHUNK):
                     part = items[a:a + _CHUNK]
+                    # one call per slot class: MPS_PRECISION_MIXED sends its
+                    # tensor-core gates to the tensor-core sweeps and the rest
+                    # to the SIMT ones ("auto": where the tuning table found
+                    # the mixed form faster for those gates)
+                    tcs = [(m, n) for _, m, n, e in part if e]
+                    prec = _native.PRECISION_PLAIN
+                    if tcs and (precision == "mixed" or _autotune.lookup(
+                            max(m for m, _ in tcs), max(n for _, n in tcs), d,
+                            len(tcs))["precision"] == "mixed"):
+                        prec = _native.PRECISION_MIXED
                     lo2 = len(rows2)
-                    rows2.extend(r for r, _, _ in part)
-                    mm, nn = max(m for _, m, _ in part), max(n for _, _, n in part)
+                    rows2.extend(r for r, _, _, _ in part)
+                    mm, nn = max(m for _, m, _, _ in part), max(n for _, _, n, _ in part)
                     tuned = (_autotune.lookup(mm, nn, d, len(part)) if autotune
                              else _autotune.DEFAULT)
                     calls.append(("2q", lo2, len(part), mm, nn, prec, tuned["lq_off"],

@@ -119,16 +119,31 @@ def test_mixed_scale_invariance(built_lib, cuda, scale):
     check_job((a, b, g, 100, True), res[0], 2)
 
 
-def test_mixed_rejects_other_jobs(built_lib, cuda):
-    """Right-canonical jobs need the accumulated V: the mixed call refuses
-    them (the Python layer sends them to a plain call)."""
+def test_mixed_call_runs_other_jobs_in_the_plain_sweeps(built_lib, cuda):
+    """One mixed call with tensor-core jobs (left-canonical, tall, 64+
+    columns) and jobs of every other kind: right-canonical (they need the
+    accumulated V), wide, and of fewer than 64 columns.  The others take the
+    SIMT sweeps of the same call: each job passes the plain path's checks, and
+    the other jobs' results equal a plain call's bit for bit."""
     rng = np.random.default_rng(3)
-    a, b, g = make_job_inputs(rng, 64, 64, 64, 2)
-    rc, _, _ = run_batch(built_lib, cuda, [(a, b, g, 64, False)], params=mixed_params())
-    assert rc == _native.MPS_ERR_ARG
-    assert "left-canonical" in _native.last_error()
-    rc, res, _ = run_batch(built_lib, cuda, [(a, b, g, 64, True)], params=mixed_params())
+    specs = []
+    for chil, chim, chir, d, k, lc in [(128, 64, 128, 2, 256, True),    # tensor-core
+                                       (64, 64, 64, 2, 64, False),      # right-canonical
+                                       (32, 64, 128, 2, 64, True),      # wide (m < n)
+                                       (16, 16, 16, 2, 32, True),       # 32 columns
+                                       (96, 96, 96, 2, 192, True)]:     # tensor-core
+        a, b, g = make_job_inputs(rng, chil, chim, chir, d, scale=1.0 / chim)
+        specs.append((a, b, g, k, lc))
+    rc, mix, p = run_batch(built_lib, cuda, specs, params=mixed_params())
     assert rc == 0, _native.last_error()
+    assert p.block_cols == 32
+    rc, pln, _ = run_batch(built_lib, cuda, specs)
+    assert rc == 0, _native.last_error()
+    for q, (spec, om, op) in enumerate(zip(specs, mix, pln)):
+        check_job(spec, om, 2)
+        if q in (1, 2, 3):
+            for key in ("a", "b", "s"):
+                assert np.array_equal(om[key], op[key]), (q, key)
 
 
 def test_mixed_needs_its_workspace_size(built_lib, cuda):
