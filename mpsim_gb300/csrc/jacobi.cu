@@ -647,7 +647,8 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
     }
 }
 
-__global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol2, const int* wait_error) {
+__global__ void sweep_end_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int njobs,
+                                 float tol2, const int* wait_error) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     // an expired round-dependency wait also marks every job's status (for
     // calls that do not read the error word back: stream capture)
@@ -655,8 +656,16 @@ __global__ void sweep_end_kernel(TwoQGeom g, int njobs, float tol2, const int* w
     if (j >= njobs) return;
     if (!g.done[j]) {
         const float o = g.offmax[j];
-        if (o > tol2) atomicAdd(g.counter, 1);
-        else g.done[j] = 1;
+        if (o > tol2) {
+            atomicAdd(g.counter, 1);
+            // mixed calls: jobs left for each sweep kernel (the host skips a
+            // kernel with none)
+            if (g.tc_mode)
+                atomicAdd(g.counter + (tc_job(jobs[j].chi_l * g.d, jobs[j].chi_r * g.d,
+                                              jobs[j].keep_left_canonical) ? 4 : 5), 1);
+        } else {
+            g.done[j] = 1;
+        }
     }
     g.offmax[j] = 0.f;
 }
@@ -685,7 +694,7 @@ __global__ void init_slots_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom 
         g.offmax[t] = 0.f;
         g.need[t] = 0;
     }
-    if (t < 4) g.counter[t] = 0;
+    if (t < 8) g.counter[t] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1388,7 +1397,7 @@ Layout make_layout(int njobs, int max_m, int max_n, bool pieces = false) {
     lo.off_off = o; o = align_up(o + nj * sizeof(float), 256);
     lo.off_done = o; o = align_up(o + nj * sizeof(int), 256);
     lo.off_need = o; o = align_up(o + nj * sizeof(int), 256);
-    lo.off_counter = o; o = align_up(o + 4 * sizeof(int), 256);
+    lo.off_counter = o; o = align_up(o + 8 * sizeof(int), 256);
     lo.off_scale = o; o = align_up(o + nj * sizeof(int), 256);
     lo.off_nrm2 = o; o = align_up(o + nj * sizeof(double), 256);
     // sweep sync: next_item, error, then block_round[njobs][nbmax] (nbmax
@@ -1557,8 +1566,12 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     int sweeps = 0;
     bool converged = false;
     if (cmax >= 2) {
+        // mixed calls: whether the last sweep left jobs for each sweep kernel
+        // (unknown, so both run, before the first read and under capture)
+        bool tc_left = true, simt_left = true;
         for (sweeps = 1; sweeps <= max_sweeps; ++sweeps) {
             MPS_CUDA_CHECK(cudaMemsetAsync(g.counter, 0, sizeof(int), s));
+            if (mixed) MPS_CUDA_CHECK(cudaMemsetAsync(g.counter + 4, 0, 2 * sizeof(int), s));
             if (cmax > 2 * bc) {
                 presort_kernel<<<njobs, PRESORT_T, sort_smem, s>>>(jobs, g, npow2, bc,
                                                                    sweeps * tbase_stride);
@@ -1576,40 +1589,47 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
                     MPS_CUDA_CHECK(cudaMemsetAsync(sync.error, 0, sizeof(int), s));
                     if (int e = tc_split_launch(jobs, njobs, g, s)) return e;
                 }
-                SweepSync tsync = sync;
-                tsync.next_item = g.counter + 2;
-                MPS_CUDA_CHECK(cudaMemsetAsync(tsync.next_item, 0, sizeof(int), s));
-                rc = tc_sweep_launch(jobs, njobs, rounds_tc, pairs_tc, g, tol2, tsync,
-                                     sweeps * tbase_stride, s);
-                if (rc) return rc;
+                if (tc_left) {
+                    SweepSync tsync = sync;
+                    tsync.next_item = g.counter + 2;
+                    MPS_CUDA_CHECK(cudaMemsetAsync(tsync.next_item, 0, sizeof(int), s));
+                    rc = tc_sweep_launch(jobs, njobs, rounds_tc, pairs_tc, g, tol2, tsync,
+                                         sweeps * tbase_stride, s);
+                    if (rc) return rc;
+                }
                 MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, sizeof(int), s));
             } else {
                 MPS_CUDA_CHECK(cudaMemsetAsync(sync.next_item, 0, 2 * sizeof(int), s));
             }
             // the SIMT jobs (all of them in the plain form): one persistent
             // launch runs every round of the sweep
-            rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, sweeps * tbase_stride, s);
-            if (rc) return rc;
-            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2, sync.error);
+            if (simt_left) {
+                rc = sweep(jobs, njobs, rounds, pairs, g, tol2, lw, sync, sweeps * tbase_stride, s);
+                if (rc) return rc;
+            }
+            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(jobs, g, njobs, tol2, sync.error);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
             if (capturing) {
                 converged = true;            // reported through the status words
                 continue;
             }
-            MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, 2 * sizeof(int),
+            // counter[0..5] (jobs left, NaN count, -, expired MMA wait, jobs
+            // left per kind) and the round-flag error word
+            MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned, g.counter, 6 * sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
-            if (mixed)
-                MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 4, g.counter + 3, sizeof(int),
-                                               cudaMemcpyDeviceToHost, s));
-            MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 2, sync.error, sizeof(int),
+            MPS_CUDA_CHECK(cudaMemcpyAsync(t_pinned + 6, sync.error, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
             MPS_CUDA_CHECK(cudaStreamSynchronize(s));
-            if (t_pinned[2] != 0)
+            if (t_pinned[6] != 0)
                 return fail(MPS_ERR_TIMEOUT, "mps_apply_2q_batch: a round-dependency wait inside the "
                                              "sweep kernel expired; results are invalid");
-            if (mixed && t_pinned[4] != 0)
+            if (mixed && t_pinned[3] != 0)
                 return fail(MPS_ERR_TIMEOUT, "mps_apply_2q_batch: a tensor-core MMA wait "
                                              "expired; results are invalid");
+            if (mixed) {
+                tc_left = t_pinned[4] != 0;
+                simt_left = t_pinned[5] != 0;
+            }
             if (t_pinned[0] == 0) {
                 converged = true;
                 break;
@@ -1822,7 +1842,7 @@ extern "C" int mps_apply_2q_batch_noalloc(void* stream, const mps_2q_job* jobs, 
                 rc = visit(jobs, njobs, pairs, g, r, tol2, lw, s);
                 if (rc) return rc;
             }
-            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(g, njobs, tol2, nullptr);
+            sweep_end_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(jobs, g, njobs, tol2, nullptr);
             MPS_LAUNCH_CHECK("sweep_end_kernel");
             MPS_CUDA_CHECK(cudaMemcpyAsync(host_counter, g.counter, sizeof(int),
                                            cudaMemcpyDeviceToHost, s));
