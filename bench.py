@@ -586,6 +586,99 @@ def run_batch_workload(args, rank, world):
     return 0
 
 
+def batched_chi256(dev, njobs=512, reps=2, check=4):
+    """The metric's own comparison: chi=256 two-qubit gates (theta 512 x 512,
+    maxsvals=256) batched njobs to a call, through mps_apply_2q_batch in the
+    plain form and in the mixed (tensor-core) form; gates/s of each, their
+    ratio, and the mixed form's accuracy against complex128 LAPACK on `check`
+    of the jobs: the truncated two-site block's infidelity, the largest
+    relative error of the kept singular values (above 1e-3 s_0) and the
+    truncation-weight error.  Synthetic sites: seeded complex Gaussians
+    (left site scaled by 1/chi), seeded Haar gates; L2 flushed before each
+    timed call."""
+    import ctypes
+    import torch
+    from mpsim_gb300 import _native
+    from mpsim_gb300.circuits import haar_random_matrix
+
+    lib = _native.load()
+    d, chi = 2, 256
+    m = n = chi * d
+    k = chi
+    gen = torch.Generator(device=dev).manual_seed(2024)
+
+    def sites(scale):
+        t = torch.randn((njobs, chi, d, chi), dtype=torch.complex64, device=dev, generator=gen)
+        return t * scale
+    A, B = sites(1.0 / chi), sites(1.0)
+    G = torch.from_numpy(np.stack([haar_random_matrix(2, d, 500 + q) for q in range(njobs)])
+                         .astype(np.complex64)).to(dev)
+    Ao = torch.empty((njobs, chi, d, k), dtype=torch.complex64, device=dev)
+    Bo = torch.empty((njobs, k, d, chi), dtype=torch.complex64, device=dev)
+    S = torch.zeros((njobs, min(m, n)), dtype=torch.float32, device=dev)   # every singular value
+    disc = torch.zeros(njobs, dtype=torch.float64, device=dev)
+    table = np.zeros(njobs, dtype=_native.JOB_DTYPE)
+    for q in range(njobs):
+        r = table[q]
+        r["a"], r["b"], r["gate"] = A[q].data_ptr(), B[q].data_ptr(), G[q].data_ptr()
+        r["a_out"], r["b_out"] = Ao[q].data_ptr(), Bo[q].data_ptr()
+        r["svals"], r["discarded"] = S[q].data_ptr(), disc[q].data_ptr()
+        r["chi_l"], r["chi_m"], r["chi_r"], r["k"], r["keep_left_canonical"] = chi, chi, chi, k, 1
+    jobs = torch.from_numpy(table.view(np.uint8)).to(dev)
+    nbytes = lib.mps_2q_workspace_bytes_mixed(njobs, m, n, d)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    out = {"config": f"{njobs} gates of theta {m} x {n}, maxsvals {k}, one call", "unit": UNIT}
+    for prec in ("plain", "mixed"):
+        p = _native.SvdParams()
+        p.precision = _native.PRECISION_MIXED if prec == "mixed" else _native.PRECISION_PLAIN
+
+        def call():
+            _native.check(lib.mps_apply_2q_batch(stream, ctypes.c_void_p(jobs.data_ptr()), njobs,
+                                                 m, n, d, ctypes.c_void_p(ws.data_ptr()), nbytes,
+                                                 ctypes.byref(p)))
+        call()
+        times = []
+        for _ in range(reps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            call()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            times.append(e0.elapsed_time(e1))
+        out[prec] = {"value": njobs / (float(np.median(times)) / 1000.0), "ms_per_call": float(np.median(times)),
+                     "sweeps": int(p.sweeps_out)}
+    out["mixed_over_plain"] = out["mixed"]["value"] / out["plain"]["value"]
+    # the mixed form's outputs (the last call) against complex128 LAPACK
+    infid, sv_err, w_err = [], [], []
+    for q in range(min(check, njobs)):
+        a = A[q].cpu().numpy().astype(np.complex128)
+        b = B[q].cpu().numpy().astype(np.complex128)
+        g = G[q].cpu().numpy().astype(np.complex128).reshape(d, d, d, d)
+        mm = (a.reshape(m, chi) @ b.reshape(chi, n)).reshape(chi, d, d, chi)
+        th = np.einsum("xyab,labr->lxyr", g, mm).reshape(m, n)
+        u, sv, vh = np.linalg.svd(th, full_matrices=False)
+        best = (u[:, :k] * sv[:k]) @ vh[:k]
+        got = Ao[q].cpu().numpy().astype(np.complex128).reshape(m, k) @ \
+            Bo[q].cpu().numpy().astype(np.complex128).reshape(k, n)
+        ov = abs(np.vdot(best, got)) ** 2 / (np.vdot(best, best).real * np.vdot(got, got).real)
+        infid.append(1.0 - ov)
+        s_gpu = S[q].cpu().numpy().astype(np.float64)[:k]
+        keep = sv[:k] > 1e-3 * sv[0]
+        sv_err.append(float(np.max(np.abs(s_gpu[keep] - sv[:k][keep]) / sv[:k][keep])))
+        wt = float(np.sum(sv[k:] ** 2))
+        w_err.append(abs(float(disc[q].item()) - wt) / max(wt, 1e-300))
+    out["mixed_accuracy_vs_fp64"] = {"jobs_checked": len(infid), "max_infidelity": max(infid),
+                                     "max_sv_rel_error": max(sv_err),
+                                     "max_truncation_weight_rel_error": max(w_err)}
+    del A, B, G, Ao, Bo, ws, flush
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_case(args):
     """Single-purpose chi=256 workloads for timing and profiling one kernel
     family (``--case``), each run ``--steps`` times after ``--warmup`` runs,
@@ -919,6 +1012,10 @@ def main():
     plan.check_status()
     graph_norm = plan_state.norm()
 
+    batched = None
+    if rank == 0 and world == 1 and args.workload == WORKLOAD:
+        batched = batched_chi256(dev)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r, why = reference_rate(circ)
@@ -972,6 +1069,8 @@ def main():
             "clocks": clk,
             "final_norm": float(norms[-1]) if norms else None,
         }
+        if batched is not None:
+            line["batched_chi256"] = batched
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
