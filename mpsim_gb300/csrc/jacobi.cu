@@ -1538,6 +1538,10 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
     const int max_chil = (max_m + d - 1) / d, max_chir = (max_n + d - 1) / d;
     int rc = merge_gate_launch(jobs, njobs, max_chil, max_chir, g, s);
     if (rc) return rc;
+    if (mixed) {
+        rc = merge_tc_launch(jobs, njobs, max_m, max_n, g, s);
+        if (rc) return rc;
+    }
     rc = scale_theta(jobs, njobs, g, s);
     if (rc) return rc;
     if (!(params && params->lq_off)) rc = lq_precondition(jobs, njobs, max_m, max_n, g, s);

@@ -36,6 +36,7 @@ merge_gate_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
     const int m = chil * d, n = d * chir;
     const bool tall = m >= n;
     const bool given = (job.flags & MPS_JOB_THETA_GIVEN) != 0;   // block-uniform
+    if (g.tc_mode && merge_on_tensor_cores(job, d)) return;       // merge_tc_kernel's job
 
     __shared__ union {
         struct { cf a[KC][TILE]; cf b[KC][TILE]; } ld;

@@ -22,6 +22,7 @@
 // density matrices) at bond dimensions where they are compute-bound: the
 // contractions of MPS.inner_product / norm (mpsim/core.py:507-565).
 #include "tc.cuh"
+#include "twoq.cuh"
 
 namespace mps {
 namespace {
@@ -53,17 +54,24 @@ struct GemmArgs {
 
 __device__ __forceinline__ void store_split8(uint8_t* base, uint32_t off, const float* v) {
     // v: 8 reals -> 16 bytes per piece at the same offset of three piece tiles
-    __align__(16) __nv_bfloat16 p0[8], p1[8], p2[8];
+    // (the paired round-to-nearest conversion: the pieces of tc::split3)
+    uint32_t w[3][4];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-        const tc::Split3 s = tc::split3(v[e]);
-        p0[e] = s.p0;
-        p1[e] = s.p1;
-        p2[e] = s.p2;
+    for (int e = 0; e < 4; ++e) {
+        const __nv_bfloat162 p0 = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
+        const float2 f0 = __bfloat1622float2(p0);
+        const float ra = v[2 * e] - f0.x, rb = v[2 * e + 1] - f0.y;
+        const __nv_bfloat162 p1 = __floats2bfloat162_rn(ra, rb);
+        const float2 f1 = __bfloat1622float2(p1);
+        const __nv_bfloat162 p2 = __floats2bfloat162_rn(ra - f1.x, rb - f1.y);
+        w[0][e] = *reinterpret_cast<const uint32_t*>(&p0);
+        w[1][e] = *reinterpret_cast<const uint32_t*>(&p1);
+        w[2][e] = *reinterpret_cast<const uint32_t*>(&p2);
     }
-    *reinterpret_cast<uint4*>(base + off) = *reinterpret_cast<const uint4*>(p0);
-    *reinterpret_cast<uint4*>(base + TC_PIECE + off) = *reinterpret_cast<const uint4*>(p1);
-    *reinterpret_cast<uint4*>(base + 2 * TC_PIECE + off) = *reinterpret_cast<const uint4*>(p2);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        *reinterpret_cast<uint4*>(base + i * TC_PIECE + off) =
+            make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
 }
 
 // Fills one stage with K chunk kc: A rows i0..i0+127, B columns j0..j0+63.
@@ -113,19 +121,17 @@ __device__ __forceinline__ void fill_stage(uint8_t* st, const GemmArgs& p, const
     }
 }
 
-__global__ void __launch_bounds__(TC_THREADS) tc_cgemm_kernel(GemmArgs p) {
+// One 128 x 64 tile of C = opA(A) opB(B) (rows i0.., columns j0..) for the
+// operands at a, b, c.  All 128 threads call it; returns false when a
+// bounded MMA wait expired (the tile is then not written).
+__device__ __forceinline__ bool cgemm_tile(const GemmArgs& p, const cf* a, const cf* b, cf* c,
+                                           int i0, int j0) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * TC_STAGE);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
-
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int z = blockIdx.z;
-    const int i0 = blockIdx.y * TC_BM, j0 = blockIdx.x * TC_BN;
-    const cf* a = p.a + (long long)z * p.bsa;
-    const cf* b = p.b + (long long)z * p.bsb;
-    cf* c = p.c + (long long)z * p.bsc;
 
     if (tid == 0) {
         mbar_init(&bar[0], 1);
@@ -206,12 +212,113 @@ __global__ void __launch_bounds__(TC_THREADS) tc_cgemm_kernel(GemmArgs p) {
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
+    return ok;
+}
+
+__global__ void __launch_bounds__(TC_THREADS) tc_cgemm_kernel(GemmArgs p) {
+    const int z = blockIdx.z;
+    (void)cgemm_tile(p, p.a + (long long)z * p.bsa, p.b + (long long)z * p.bsb,
+                     p.c + (long long)z * p.bsc, blockIdx.y * TC_BM, blockIdx.x * TC_BN);
+}
+
+// The two-site merge of the mixed form's tensor-core jobs (tc_job, theta not
+// given): M = A B per job, A = (chi_l d) x chi_m row-major, B = chi_m x
+// (d chi_r) row-major, written column-major into the job's Jacobi matrix X
+// (leading dimension lslot); merge_gate_tc_kernel then mixes M with the gate
+// in place.  Grid: (column tiles, row tiles, jobs) of the largest job.
+__global__ void __launch_bounds__(TC_THREADS)
+merge_tc_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g) {
+    const mps_2q_job job = jobs[blockIdx.z];
+    const int d = g.d;
+    const int m = job.chi_l * d, n = d * job.chi_r;
+    if (!merge_on_tensor_cores(job, d)) return;
+    const int i0 = blockIdx.y * TC_BM, j0 = blockIdx.x * TC_BN;
+    if (i0 >= m || j0 >= n) return;
+    GemmArgs p;
+    p.m = m; p.n = n; p.k = job.chi_m;
+    p.a = reinterpret_cast<const cf*>(job.a); p.sam = job.chi_m; p.sak = 1; p.conj_a = 0;
+    p.b = reinterpret_cast<const cf*>(job.b); p.sbk = n; p.sbn = 1; p.conj_b = 0;
+    cf* X = g.X + (size_t)blockIdx.z * g.lslot * g.cslot;
+    p.c = X; p.scm = 1; p.scn = g.lslot;
+    p.bsa = p.bsb = p.bsc = 0;
+    if (!cgemm_tile(p, p.a, p.b, X, i0, j0) && threadIdx.x == 0) atomicOr(g.counter + 3, 1);
+}
+
+// theta[(l,a'),(b',r)] = sum_{a,b} G[(a'b'),(ab)] M[(l,a),(b,r)] in place in
+// X for the jobs merge_tc_kernel took, and its copy in T (their right factor
+// comes from U^H theta).  One thread per (job, l, r).
+template <int D>
+__device__ __forceinline__ void gate_block(cf* X, cf* T, const cf* G, int l, int r, int chir,
+                                           int lslot) {
+    cf mloc[D * D];
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int b = 0; b < D; ++b) mloc[a * D + b] = X[(size_t)(b * chir + r) * lslot + (l * D + a)];
+#pragma unroll
+    for (int ap = 0; ap < D; ++ap)
+#pragma unroll
+        for (int bp = 0; bp < D; ++bp) {
+            const cf* grow = G + (size_t)(ap * D + bp) * D * D;
+            cf th = cmake(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < D * D; ++q)
+                cfma(th, __ldg(reinterpret_cast<const float2*>(grow + q)), mloc[q]);
+            const size_t off = (size_t)(bp * chir + r) * lslot + (l * D + ap);
+            X[off] = th;
+            T[off] = th;
+        }
+}
+
+__global__ void __launch_bounds__(256)
+merge_gate_tc_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int max_lr) {
+    const mps_2q_job job = jobs[blockIdx.y];
+    const int d = g.d;
+    if (!merge_on_tensor_cores(job, d)) return;
+    const int chil = job.chi_l, chir = job.chi_r;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= max_lr || e >= chil * chir) return;
+    const int l = e / chir, r = e - (e / chir) * chir;
+    cf* X = g.X + (size_t)blockIdx.y * g.lslot * g.cslot;
+    cf* T = g.T + (size_t)blockIdx.y * g.lslot * g.cslot;
+    const cf* G = reinterpret_cast<const cf*>(job.gate);
+    if (d == 2) gate_block<2>(X, T, G, l, r, chir, g.lslot);
+    else if (d == 3) gate_block<3>(X, T, G, l, r, chir, g.lslot);
+    else gate_block<4>(X, T, G, l, r, chir, g.lslot);
 }
 
 }  // namespace
 }  // namespace mps
 
 using namespace mps;
+
+namespace mps {
+
+int merge_tc_launch(const mps_2q_job* jobs, int njobs, int max_m, int max_n, const TwoQGeom& g,
+                    cudaStream_t s) {
+    if (njobs <= 0 || g.d > 4) return MPS_OK;   // (the SIMT merge takes d > 4)
+    static KernelSetup ks;
+    int dev = 0;
+    MPS_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(MPS_ERR_ARG, "device index beyond 63");
+    std::call_once(ks.once[dev], [&] {
+        cudaError_t e = cudaFuncSetAttribute(merge_tc_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)TC_SMEM);
+        ks.rc[dev] = e == cudaSuccess ? MPS_OK : cuda_fail(e, "cudaFuncSetAttribute(merge_tc_kernel)");
+    });
+    if (ks.rc[dev] != MPS_OK) return ks.rc[dev];
+    dim3 grid((max_n + TC_BN - 1) / TC_BN, (max_m + TC_BM - 1) / TC_BM, njobs);
+    merge_tc_kernel<<<grid, TC_THREADS, TC_SMEM, s>>>(jobs, g);
+    MPS_LAUNCH_CHECK("merge_tc_kernel");
+    const int max_lr = (max_m / g.d) * (max_n / g.d);
+    dim3 gg((max_lr + 255) / 256, njobs);
+    merge_gate_tc_kernel<<<gg, 256, 0, s>>>(jobs, g, max_lr);
+    MPS_LAUNCH_CHECK("merge_gate_tc_kernel");
+    return MPS_OK;
+}
+
+}  // namespace mps
 
 extern "C" int mps_cgemm_tc(void* stream, int m, int n, int k, const mps_c64* a, long long sam,
                             long long sak, int conj_a, const mps_c64* b, long long sbk,

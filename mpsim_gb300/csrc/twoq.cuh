@@ -73,6 +73,13 @@ __host__ __device__ __forceinline__ bool tc_job(int m, int n, int keep_left_cano
     return !job_tracks_v(m, n, keep_left_canonical) && (m < n ? m : n) >= 64;
 }
 
+// ... and whose merge runs on the tensor cores as well (theta not given;
+// qudits of up to 4 levels: the gate step keeps a d^2 block in registers).
+__host__ __device__ __forceinline__ bool merge_on_tensor_cores(const mps_2q_job& job, int d) {
+    return d <= 4 && tc_job(job.chi_l * d, job.chi_r * d, job.keep_left_canonical) &&
+           (job.flags & MPS_JOB_THETA_GIVEN) == 0;
+}
+
 // Singular values at or below this (relative to max(s_0, 1)) are treated as
 // exact zeros: the isometric factor gets an orthonormal completion there.
 constexpr float kZeroSigma = 1e-30f;
@@ -94,6 +101,11 @@ int tc_sweep_launch(const mps_2q_job* jobs, int njobs, int rounds, int pairs, co
 int tc_split_launch(const mps_2q_job* jobs, int njobs, const TwoQGeom& g, cudaStream_t s);
 int tc_merge_launch(const mps_2q_job* jobs, int njobs, const TwoQGeom& g, cudaStream_t s);
 
+// The mixed form's merge of the merge_on_tensor_cores() jobs (tcgemm.cu): M =
+// A B on tcgen05 (split bf16, FP32-grade) into X, then the gate mixed in
+// place and copied to T.  The SIMT merge skips those jobs in such a call.
+int merge_tc_launch(const mps_2q_job* jobs, int njobs, int max_m, int max_n, const TwoQGeom& g,
+                    cudaStream_t s);
 int merge_gate_launch(const mps_2q_job* jobs, int njobs, int max_chil, int max_chir,
                       const TwoQGeom& g, cudaStream_t s);
 
