@@ -335,6 +335,10 @@ class MPS:
         self._pending_sites = set()
         self._pending_1q = []            # (site, d x d complex64 gate) waiting for one launch
         self._pending_1q_sites = set()
+        # per-job status words of earlier two-qudit calls, copied to pinned
+        # host memory behind each call and checked once the copy is done
+        self._status_pending = []
+        self._status_free = []           # pinned buffers of checked calls, reused
         # bumped whenever a site tensor is replaced; is_valid caches per value
         self._version = 0
         self._valid_at = (-1, False)
@@ -536,7 +540,9 @@ class MPS:
         _native.check(self._lib().mps_wavefunction(
             self._stream(), _ptr_array(self._sites), _int_array(chis), n, d,
             ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ws.data_ptr()), ws.numel()))
-        return out.cpu().numpy()
+        res = out.cpu().numpy()
+        self._check_status(block=True)
+        return res
 
     def amplitudes(self, bitstrings) -> np.ndarray:
         """<x|psi> for each row of ``bitstrings`` (shape (S, nqudits))."""
@@ -558,7 +564,9 @@ class MPS:
             self._stream(), _ptr_array(self._sites), _int_array(chis), self._nqudits, d,
             ctypes.c_void_p(bdev.data_ptr()), nb, ctypes.c_void_p(out.data_ptr()),
             ctypes.c_void_p(ws.data_ptr()), ws.numel()))
-        return out.cpu().numpy()
+        res = out.cpu().numpy()
+        self._check_status(block=True)
+        return res
 
     def dagger(self) -> None:
         """Conjugates every site (core.py:502-505)."""
@@ -594,7 +602,29 @@ class MPS:
 
     def norm(self) -> float:
         """sqrt(Re <self|self>) (core.py:563-565)."""
-        return np.sqrt(self.inner_product(self).real)
+        n = np.sqrt(self.inner_product(self).real)
+        self._check_status(block=True)
+        return n
+
+    def _check_status(self, block: bool) -> None:
+        """Raises NativeError(MPS_ERR_NONFINITE) for a finished two-qudit call
+        whose per-job status words report a NaN/Inf singular value that first
+        appeared after the call returned (one in theta, a sweep cap or an
+        expired wait the call reports itself).  block=False looks only at the
+        calls whose status copy has completed."""
+        keep = []
+        for st_host, ev in self._status_pending:
+            if not block and not ev.query():
+                keep.append((st_host, ev))
+                continue
+            ev.synchronize()
+            bits = int(np.bitwise_or.reduce(st_host.numpy())) if st_host.numel() else 0
+            if bits & _native.STATUS_NONFINITE:
+                self._status_pending = []
+                raise _native.NativeError(_native.MPS_ERR_NONFINITE,
+                                          "a two-qudit gate produced a NaN/Inf singular value")
+            self._status_free.append(st_host)
+        self._status_pending = keep
 
     def renormalize(self, to_norm: float = 1.0) -> None:
         """Scales every site by (to_norm / norm)^(1/n) (core.py:567-594)."""
@@ -1036,6 +1066,20 @@ class MPS:
             ev1.record(torch.cuda.current_stream(dev))
             timing.append((njobs, max_m, max_n, self.svd_params.sweeps_out, ev0, ev1))
         _check_svd_rc(rc, self.on_unconverged)
+        self._check_status(block=False)
+        # the call returns before its last kernels: a NaN/Inf that first
+        # appears after the first sweep only shows in the status words, read
+        # here behind the call (no synchronisation)
+        st_host = next((b for b in self._status_free if b.numel() >= njobs), None)
+        if st_host is None:
+            st_host = torch.empty(max(njobs, 64), dtype=torch.int32, pin_memory=True)
+        else:
+            self._status_free.remove(st_host)
+        st_host[njobs:].zero_()
+        st_host[:njobs].copy_(status, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(dev))
+        self._status_pending.append((st_host, ev))
         for left, a_out, b_out in outs:
             self._sites[left] = a_out
             self._version += 1

@@ -79,6 +79,13 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t
     return d;
 }
 
+// The descriptor of the operand byte_off bytes further (a multiple of 16):
+// the start address field is linear and, for shared memory below 256 KB,
+// never carries out of its 14 bits.
+__device__ __forceinline__ uint64_t sdesc_add(uint64_t d, uint32_t byte_off) {
+    return d + (uint64_t)(byte_off >> 4);
+}
+
 // Instruction descriptor of tcgen05.mma.kind::f16 with bf16 A and B and an
 // FP32 accumulator: D format F32 (1) at [4,6), A format BF16 (1) at [7,10),
 // B format BF16 (1) at [10,13), A / B MN-major flags at bits 15 / 16,

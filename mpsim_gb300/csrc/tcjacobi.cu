@@ -361,7 +361,7 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             __syncthreads();
             if (tid == 0) {
                 tc::fence_after_sync();
-                const uint32_t s0 = tc::smem_u32(tile);
+                const uint64_t d0 = tc::sdesc(tc::smem_u32(tile), 16, 1024);
                 // piece products smallest first: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)
                 const int pa[6] = {2, 1, 0, 1, 0, 0};
                 const int pb[6] = {0, 1, 2, 0, 1, 0};
@@ -370,8 +370,8 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
 #pragma unroll
                     for (int q = 0; q < 6; ++q)
                         tc::mma_bf16(tmem + 64u * b,
-                                     tc::sdesc(s0 + pa[q] * TJ_PIECE + ks * 32, 16, 1024),
-                                     tc::sdesc(s0 + pb[q] * TJ_PIECE + ks * 32, 16, 1024), IDESC_G,
+                                     tc::sdesc_add(d0, pa[q] * TJ_PIECE + ks * 32),
+                                     tc::sdesc_add(d0, pb[q] * TJ_PIECE + ks * 32), IDESC_G,
                                      (ks | q) != 0);
                 tc::mma_commit(&ax.bar[b]);
             }
@@ -615,7 +615,8 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             __syncthreads();
             if (tid == 0) {
                 tc::fence_after_sync();
-                const uint32_t sa = tc::smem_u32(At), sb = tc::smem_u32(smem);
+                const uint64_t da = tc::sdesc(tc::smem_u32(At), TJ_MGRP, 1024);
+                const uint64_t db = tc::sdesc(tc::smem_u32(smem), 16, 1024);
                 // piece products smallest first: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)
                 const int pa[6] = {2, 1, 0, 1, 0, 0};
                 const int pb[6] = {0, 1, 2, 0, 1, 0};
@@ -623,8 +624,8 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                 for (int q = 0; q < 6; ++q)
 #pragma unroll
                     for (int ks = 0; ks < 4; ++ks)
-                        tc::mma_bf16(tmem, tc::sdesc(sa + pa[q] * TJ_PIECE + ks * 2048, TJ_MGRP, 1024),
-                                     tc::sdesc(sb + pb[q] * TJ_PIECE + ks * 32, 16, 1024), IDESC_U,
+                        tc::mma_bf16(tmem, tc::sdesc_add(da, pa[q] * TJ_PIECE + ks * 2048),
+                                     tc::sdesc_add(db, pb[q] * TJ_PIECE + ks * 32), IDESC_U,
                                      (q | ks) != 0);
                 tc::mma_commit(&ax.bar[0]);
             }

@@ -190,3 +190,34 @@ def test_shape_plan_and_cost_shards():
     assert sorted(i for s in shards for i in s) == list(range(8))
     assert C.shard_by_cost(batch, 1) == [list(range(8))]
     assert [len(s) for s in C.shard_by_cost(batch[:2], 4)].count(0) == 2
+
+
+def test_status_words_checked_after_the_call():
+    """MPS._check_status: a finished call whose status words report a NaN/Inf
+    raises MPS_ERR_NONFINITE; an unfinished one is kept for later unless the
+    check blocks; clean ones recycle their host buffer."""
+    import types
+    import torch
+    from mpsim_gb300 import _native
+    from mpsim_gb300.core import MPS
+
+    class Ev:
+        def __init__(self, done):
+            self.done = done
+
+        def query(self):
+            return self.done
+
+        def synchronize(self):
+            self.done = True
+
+    me = types.SimpleNamespace(_status_pending=[], _status_free=[])
+    clean = torch.zeros(4, dtype=torch.int32)
+    bad = torch.tensor([0, _native.STATUS_NONFINITE, 0, 0], dtype=torch.int32)
+    me._status_pending = [(clean, Ev(True)), (bad, Ev(False))]
+    MPS._check_status(me, block=False)              # the unfinished one waits
+    assert len(me._status_pending) == 1 and me._status_free == [clean]
+    with pytest.raises(_native.NativeError) as ei:
+        MPS._check_status(me, block=True)
+    assert ei.value.code == _native.MPS_ERR_NONFINITE
+    assert me._status_pending == []
