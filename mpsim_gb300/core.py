@@ -23,10 +23,11 @@ Differences from the reference, all deliberate:
   device error of a queued gate is raised by the call that runs the queue;
 * ``get_node(s)`` return host copies (TensorNetwork-like nodes with the
   reference's initial axis order: physical axis first);
-* ``from_wavefunction`` returns the reference's state in the left-canonical
-  gauge (TensorNetwork's split_node puts sqrt(S) on both sides) and takes
-  at most d^(nqudits-1) = 1792 amplitudes per row of its first split (the
-  Jacobi kernel's register-held column length: 11 qubits, 7 qutrits);
+* ``from_wavefunction`` returns the reference's state in a mixed-canonical
+  gauge (TensorNetwork's split_node puts sqrt(S) on both sides); its middle
+  bond must stay below the Jacobi kernel's register-held column length of
+  1792 (21 qubits, 13 qutrits), longer splits are compressed by column
+  blocks first;
 * ``sample`` draws from the same single-site marginals with the same NumPy
   global-RNG calls as the reference, computing all marginals in one device
   pass instead of one full contraction per site and sample.
@@ -164,41 +165,95 @@ def _check_svd_rc(rc: int, on_unconverged: str = "raise") -> None:
     raise _native.NativeError(rc, _native.last_error())
 
 
-def _given_svd(device, stream, mat, left_canonical: bool, on_unconverged: str = "raise"):
-    """Thin SVD of a device matrix ``mat`` (m x n complex64, row-major) with
-    the two-qudit kernel's given-matrix jobs (MPS_JOB_THETA_GIVEN, d = 1), keeping all
-    r = min(m, n) values.  Returns (left (m, r), right (r, n), singular values
-    (r,) float32 on the host): left = U, right = S V^H when left_canonical,
-    else left = U S, right = V^H."""
+def _given_svd_batch(device, stream, mats, left_canonical: bool, on_unconverged: str = "raise"):
+    """Thin SVDs of nb device matrices of one shape (``mats``: nb x m x n
+    complex64, each row-major) in one call of the two-qudit kernel's
+    given-matrix jobs (MPS_JOB_THETA_GIVEN, d = 1), keeping all r = min(m, n)
+    values.  Returns (left (nb, m, r), right (nb, r, n), singular values
+    (nb, r) float32 on the device): left = U, right = S V^H when
+    left_canonical, else left = U S, right = V^H."""
     lib = _native.load()
-    m, n = (int(x) for x in mat.shape)
+    nb, m, n = (int(x) for x in mats.shape)
     if max(m, n) > MAX_SVD_LENGTH:
         raise NotImplementedError(
             f"a {m} x {n} matrix is longer than the {MAX_SVD_LENGTH} rows the Jacobi SVD kernel "
             f"holds")
     r = min(m, n)
-    mat = mat.contiguous()
-    a_out = torch.empty((m, 1, r), dtype=torch.complex64, device=device)
-    b_out = torch.empty((r, 1, n), dtype=torch.complex64, device=device)
-    sv = torch.zeros(max(r, 1), dtype=torch.float32, device=device)
-    status = torch.zeros(1, dtype=torch.int32, device=device)
-    table = np.zeros(1, dtype=_native.JOB_DTYPE)
-    row = table[0]
-    row["a"], row["b"], row["gate"] = mat.data_ptr(), 0, 0
-    row["flags"] = _native.JOB_THETA_GIVEN
-    row["a_out"] = a_out.data_ptr() if a_out.numel() else 0
-    row["b_out"] = b_out.data_ptr() if b_out.numel() else 0
-    row["svals"], row["status"] = sv.data_ptr(), status.data_ptr()
-    row["chi_l"], row["chi_m"], row["chi_r"], row["k"] = m, n, n, r
-    row["keep_left_canonical"] = 1 if left_canonical else 0
+    mats = mats.contiguous()
+    a_out = torch.empty((nb, m, r), dtype=torch.complex64, device=device)
+    b_out = torch.empty((nb, r, n), dtype=torch.complex64, device=device)
+    sv = torch.zeros((nb, max(r, 1)), dtype=torch.float32, device=device)
+    status = torch.zeros(nb, dtype=torch.int32, device=device)
+    table = np.zeros(nb, dtype=_native.JOB_DTYPE)
+    for b in range(nb):
+        row = table[b]
+        row["a"], row["b"], row["gate"] = mats[b].data_ptr(), 0, 0
+        row["flags"] = _native.JOB_THETA_GIVEN
+        row["a_out"] = a_out[b].data_ptr() if a_out.numel() else 0
+        row["b_out"] = b_out[b].data_ptr() if b_out.numel() else 0
+        row["svals"], row["status"] = sv[b].data_ptr(), status[b].data_ptr()
+        row["chi_l"], row["chi_m"], row["chi_r"], row["k"] = m, n, n, r
+        row["keep_left_canonical"] = 1 if left_canonical else 0
     jobs = torch.from_numpy(table.view(np.uint8)).to(device)
-    nbytes = lib.mps_2q_workspace_bytes(1, m, n, 1)
+    nbytes = lib.mps_2q_workspace_bytes(nb, m, n, 1)
     ws = _WS.get(device, nbytes, "2q")
-    rc = lib.mps_apply_2q_batch(stream, ctypes.c_void_p(jobs.data_ptr()), 1, m, n, 1,
+    rc = lib.mps_apply_2q_batch(stream, ctypes.c_void_p(jobs.data_ptr()), nb, m, n, 1,
                                 ctypes.c_void_p(ws.data_ptr()), ws.numel(),
                                 ctypes.byref(_native.SvdParams()))
     _check_svd_rc(rc, on_unconverged)
-    return a_out.view(m, r), b_out.view(r, n), sv.cpu().numpy()[:r]
+    return a_out, b_out, sv[:, :r]
+
+
+def _given_svd(device, stream, mat, left_canonical: bool, on_unconverged: str = "raise"):
+    """Thin SVD of a device matrix ``mat`` (m x n complex64, row-major); see
+    _given_svd_batch.  Returns (left (m, r), right (r, n), singular values
+    (r,) float32 on the host)."""
+    m, n = (int(x) for x in mat.shape)
+    left, right, sv = _given_svd_batch(device, stream, mat.reshape(1, m, n), left_canonical,
+                                       on_unconverged)
+    return left[0], right[0], sv[0].cpu().numpy()
+
+
+def _wide_left_svd(device, stream, mat):
+    """Left factor and remainder of a wide or square device matrix ``mat``
+    (m x n complex64, row-major, m <= n): U (m x m, orthonormal columns) and
+    U^H mat = S V^H (m x n), every value kept -- what one cut of
+    from_wavefunction needs.  Matrices within the Jacobi kernel's length go
+    to it directly.  A longer one (n > MAX_SVD_LENGTH, m < MAX_SVD_LENGTH) is
+    first compressed by columns: mat = [B_1 .. B_t] with blocks of
+    MAX_SVD_LENGTH columns (the last one shorter), each replaced by its U_i S_i
+    (m x min(m, width)), which leaves mat mat^H = sum B_i B_i^H -- and so U
+    and S -- unchanged; the blocks of one width go through one batched call,
+    and the compression repeats until the matrix fits.  U is then the left
+    factor of the compressed matrix and the remainder one GEMM against mat."""
+    m, n = (int(x) for x in mat.shape)
+    if n <= MAX_SVD_LENGTH:
+        left, right, _ = _given_svd(device, stream, mat, True)
+        return left, right
+    if m >= MAX_SVD_LENGTH:
+        raise NotImplementedError(
+            f"a {m} x {n} matrix has both sides at or above the {MAX_SVD_LENGTH} rows the "
+            f"Jacobi SVD kernel holds")
+    ell = MAX_SVD_LENGTH
+    c = mat.contiguous()
+    while int(c.shape[1]) > ell:
+        w = int(c.shape[1])
+        full, tail = divmod(w, ell)
+        parts = []
+        if full:
+            blocks = c[:, :full * ell].reshape(m, full, ell).permute(1, 0, 2)
+            us, _, _ = _given_svd_batch(device, stream, blocks, False)
+            parts.append(us.permute(1, 0, 2).reshape(m, full * m))
+        if tail:
+            us, _, _ = _given_svd(device, stream, c[:, full * ell:].contiguous(), False)
+            parts.append(us)
+        c = torch.cat(parts, dim=1).contiguous() if len(parts) > 1 else parts[0].contiguous()
+    u, _, _ = _given_svd(device, stream, c, True)
+    u = u.contiguous()
+    rest = torch.empty((m, n), dtype=torch.complex64, device=device)
+    _cgemm(_native.load(), stream, m, n, m, u, 0, 1, m, True, mat, 0, n, 1, False,
+           rest, 0, n, 1)
+    return u, rest
 
 
 def kept_by_truncation_error(svals: np.ndarray, max_truncation_err: float) -> int:
@@ -745,11 +800,15 @@ class MPS:
     def from_wavefunction(wavefunction, nqudits: int, qudit_dimension: int = 2,
                           tensor_prefix: str = "q") -> "MPS":
         """MPS of a state vector by successive SVDs across every cut, all
-        singular values kept (core.py:245-328).  The state is the reference's;
-        the gauge is left-canonical (U on each site, S V^H carried right)
-        where TensorNetwork's split_node puts sqrt(S) on both sides.  Every
-        split runs through the Jacobi SVD kernel, so d^(nqudits-1) must not
-        exceed its 1792-row limit (11 qubits, 7 qutrits)."""
+        singular values kept (core.py:245-328): the reference's state and bond
+        dimensions min(d^i, d^(n-i)).  The gauge differs (TensorNetwork's
+        split_node puts sqrt(S) on both sides): the cuts left of the middle
+        site are split from the left (U on each site, S V^H carried right),
+        the others from the right end on the conjugate transpose (V^H on each
+        site, U S carried left), so that every split is of a wide matrix whose
+        short side is the bond (_wide_left_svd).  The middle cut's bond must
+        stay below the Jacobi kernel's 1792 rows: up to 21 qubits or 13
+        qutrits."""
         if not isinstance(wavefunction, (list, tuple, np.ndarray)):
             raise TypeError("Invalid type for wavefunction.")
         wavefunction = np.array(wavefunction)
@@ -763,19 +822,37 @@ class MPS:
                 "Mismatch between wavefunction, qudit_dimension, and nqudits. "
                 f"Expected {d ** nqudits} elements in the wavefunction, but wavefunction has "
                 f"{wavefunction.size} elements.")
+        middle = nqudits // 2
+        if d ** middle >= MAX_SVD_LENGTH:
+            raise NotImplementedError(
+                f"the middle bond of {nqudits} qudits of dimension {d} reaches the "
+                f"{MAX_SVD_LENGTH} rows the Jacobi SVD kernel holds")
         mps = MPS(nqudits, d, tensor_prefix)
         dev, stream = mps._device, mps._stream()
         rest = torch.from_numpy(np.ascontiguousarray(wavefunction.astype(np.complex64))).to(dev)
+        # sites 0 .. middle-1 from the left: rest (chi*d x d^(n-1-i)) = U . S V^H
         chi = 1
         sites = []
-        for i in range(nqudits - 1):
-            left, right, _ = _given_svd(dev, stream, rest.view(chi * d, d ** (nqudits - 1 - i)),
-                                        True)
-            k = int(left.shape[1])
-            sites.append(left.reshape(chi, d, k))
-            rest = right
+        for i in range(middle):
+            u, rest = _wide_left_svd(dev, stream, rest.reshape(chi * d, d ** (nqudits - 1 - i)))
+            k = int(u.shape[1])
+            sites.append(u.reshape(chi, d, k))
             chi = k
-        sites.append(rest.reshape(chi, d, 1))
+        # sites n-1 .. middle+1 from the right: rest (rows x d*chir) = (U S) . V^H,
+        # from the wide split of its conjugate transpose: rest^H = V . (S U^H)
+        chir = 1
+        right_sites = []
+        rows = int(rest.numel()) // d
+        for j in range(nqudits - 1, middle, -1):
+            mat = rest.reshape(rows, d * chir)
+            v, sut = _wide_left_svd(dev, stream, mat.conj().T.contiguous())
+            k = int(v.shape[1])
+            right_sites.append(v.conj().T.contiguous().reshape(k, d, chir))
+            rest = sut.conj().T.contiguous()          # rows x k: U S
+            chir = k
+            rows //= d
+        sites.append(rest.reshape(chi, d, chir))
+        sites.extend(reversed(right_sites))
         mps._sites = sites
         return mps
 

@@ -119,8 +119,37 @@ def test_from_wavefunction_errors_and_limit(cuda):
     m = MPS.from_wavefunction(psi, 5)
     assert np.allclose(m.wavefunction(), psi, atol=1e-6)
     assert list(m.bond_dimensions()) == [2, 4, 4, 2]
+    # the middle bond (2^11) reaches the Jacobi kernel's 1792 rows
     with pytest.raises(NotImplementedError):
-        MPS.from_wavefunction(np.ones(2 ** 12) / 64.0, 12)
+        MPS.from_wavefunction(np.ones(2 ** 22) / 2048.0, 22)
+
+
+@pytest.mark.parametrize("n,d,kind", [(14, 2, "haar"), (16, 2, "product"), (9, 3, "haar"),
+                                      (13, 2, "ghz"), (21, 2, "haar"), (13, 3, "ghz")])
+def test_from_wavefunction_long_splits(cuda, n, d, kind):
+    """States whose splits are longer than the Jacobi kernel's 1792 rows (the
+    column-block compression of _wide_left_svd): the state comes back, with
+    the reference's bond dimensions min(d^i, d^(n-i)) (all values kept, as
+    split_node does, zeros included)."""
+    rng = np.random.default_rng(n * 10 + d)
+    size = d ** n
+    if kind == "haar":
+        psi = (rng.normal(size=size) + 1j * rng.normal(size=size)).astype(np.complex64)
+    elif kind == "product":
+        psi = np.zeros(size, np.complex64)
+        psi[int(rng.integers(size))] = 1.0
+    else:
+        psi = np.zeros(size, np.complex64)
+        psi[0] = psi[-1] = 1.0
+    psi /= np.linalg.norm(psi)
+    m = MPS.from_wavefunction(psi, n, d)
+    assert list(m.bond_dimensions()) == [min(d ** i, d ** (n - i)) for i in range(1, n)]
+    wf = m.wavefunction().reshape(-1)
+    a, b = psi.astype(np.complex128), wf.astype(np.complex128)
+    fid = abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+    assert fid > 1.0 - 1e-9
+    assert np.max(np.abs(wf - psi)) < 4e-6
+    assert m.is_valid()
 
 
 def test_orthonormalize(cuda, z):
