@@ -560,6 +560,8 @@ sweep_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, float tol2, int nj
     extern __shared__ float2 smem[];
     __shared__ float s_off[BC];
     __shared__ int s_item, s_abort, s_skip;
+    // a mixed call whose jobs all take the tensor-core sweeps: nothing to claim
+    if (g.tc_mode && __ldcg(g.counter + 6) == 0) return;
     // ring hand-off barriers, one per (step < BC-1, visitor); see
     // visit_ring_handoff
     __shared__ __align__(8) uint64_t s_bar[(BC - 1) * BC];
@@ -695,6 +697,15 @@ __global__ void init_slots_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom 
         g.need[t] = 0;
     }
     if (t < 8) g.counter[t] = 0;
+}
+
+// counter[6] = the jobs of a mixed call that take the SIMT sweeps (counted
+// once, after init_slots_kernel cleared the counters; nothing resets it)
+__global__ void count_simt_jobs_kernel(const mps_2q_job* __restrict__ jobs, int d, int njobs,
+                                       int* counter) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < njobs && !tc_job(jobs[t].chi_l * d, jobs[t].chi_r * d, jobs[t].keep_left_canonical))
+        atomicAdd(counter + 6, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -1534,6 +1545,10 @@ extern "C" int mps_apply_2q_batch(void* stream, const mps_2q_job* jobs, int njob
         blocks = max(blocks, (njobs + 255) / 256);
         init_slots_kernel<<<blocks, 256, 0, s>>>(jobs, g, njobs);
         MPS_LAUNCH_CHECK("init_slots_kernel");
+        if (mixed) {
+            count_simt_jobs_kernel<<<(njobs + 255) / 256, 256, 0, s>>>(jobs, d, njobs, g.counter);
+            MPS_LAUNCH_CHECK("count_simt_jobs_kernel");
+        }
     }
     const int max_chil = (max_m + d - 1) / d, max_chir = (max_n + d - 1) / d;
     int rc = merge_gate_launch(jobs, njobs, max_chil, max_chir, g, s);

@@ -28,7 +28,9 @@ struct TwoQGeom {
     int* done;        // njobs: 1 once a sweep made no rotation
     int* need;        // njobs: kept columns that need an orthonormal completion
     int* counter;     // [0] jobs still rotating, [1] jobs with NaN/Inf, [2] the tensor-core
-                      // sweep's item counter, [3] an expired wait (MMA or round flag)
+                      // sweep's item counter, [3] an expired wait (MMA or round flag),
+                      // [4] / [5] tensor-core / SIMT jobs left after a sweep (mixed
+                      // calls), [6] SIMT jobs of a mixed call
     int* cmap;        // njobs * cslot: physical column at each sorted position
     float* cnrm;      // njobs * cslot: squared norm of each physical column
     int* scale;       // njobs: theta was multiplied by 2^scale[j] before the SVD
