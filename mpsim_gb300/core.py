@@ -1200,28 +1200,79 @@ class MPS:
         """Applies operations in order (core.py:1221-1276), each through
         apply_one_qudit_gate / apply_two_qudit_gate: two-qudit gates on
         disjoint adjacent pairs join the state's queue and run as one batched
-        launch, so the result equals in-order application."""
+        launch, so the result equals in-order application.  Consecutive
+        two-qudit operations whose site ranges (all sites from the lower to
+        the higher index, which a non-adjacent gate's SWAP chains cross) are
+        disjoint are interleaved step by step (_two_qudit_steps), so that
+        the k-th SWAP of every chain joins one launch; each chain keeps its
+        own order and touches no other chain's sites, so the result is the
+        in-order one.  An operation that fails validation first lets the
+        operations before it run, as in-order application would.  With
+        track_norms every operation runs on its own (the norm history is
+        per operation)."""
         try:
             operations = iter(operations)
         except TypeError:
             operations = (operations,)
-        for op in operations:
-            if not isinstance(op, MPSOperation):
-                raise TypeError("Argument operation should be of type MPSOperation but is "
-                                f"of type {type(op)}.")
-            if not op.is_valid():
-                raise ValueError("Input MPS Operation is not valid.")
-            if op.is_single_qudit_operation():
-                (i,) = op.qudit_indices
-                self.apply_one_qudit_gate(op.node(copy=False), i, **kwargs)
-            elif op.is_two_qudit_operation():
-                i, j = op.qudit_indices
-                self.apply_two_qudit_gate(op.node(copy=False), i, j, **kwargs)
-            else:
-                raise ValueError(
-                    "Only one-qudit and two-qudit gates are supported. To apply a gate on three or "
-                    "more qudits, the gate must be compiled into a sequence of one- and two-qudit "
-                    "gates.")
+        group = []                        # step lists of two-qudit operations
+        used = set()                      # the sites their ranges cover
+
+        def run_group():
+            chains = list(group)
+            group.clear()
+            used.clear()
+            for t in range(max((len(c) for c in chains), default=0)):
+                for c in chains:
+                    if t < len(c):
+                        c[t]()
+
+        try:
+            for op in operations:
+                if not isinstance(op, MPSOperation):
+                    raise TypeError("Argument operation should be of type MPSOperation but is "
+                                    f"of type {type(op)}.")
+                if not op.is_valid():
+                    raise ValueError("Input MPS Operation is not valid.")
+                if op.is_single_qudit_operation():
+                    run_group()
+                    (i,) = op.qudit_indices
+                    self.apply_one_qudit_gate(op.node(copy=False), i, **kwargs)
+                elif op.is_two_qudit_operation():
+                    i, j = op.qudit_indices
+                    if self.track_norms:
+                        run_group()
+                        self.apply_two_qudit_gate(op.node(copy=False), i, j, **kwargs)
+                        continue
+                    node = op.node(copy=False)
+                    self._check_two_qudit(node, i, j)
+                    span = set(range(min(i, j), max(i, j) + 1))
+                    if span & used:
+                        run_group()
+                    group.append(self._two_qudit_steps(node, i, j, kwargs))
+                    used.update(span)
+                else:
+                    raise ValueError(
+                        "Only one-qudit and two-qudit gates are supported. To apply a gate on "
+                        "three or more qudits, the gate must be compiled into a sequence of one- "
+                        "and two-qudit gates.")
+        except BaseException:
+            run_group()
+            raise
+        run_group()
+
+    def _two_qudit_steps(self, gate, i: int, j: int, kwargs) -> list:
+        """apply_two_qudit_gate(gate, i, j) as its sequence of adjacent steps
+        (core.py:1034-1058): SWAPs carrying the lower site up to the higher
+        one's neighbour, the gate there (in the caller's orientation), SWAPs
+        back."""
+        lo, hi = min(i, j), max(i, j)
+        steps = [lambda a=a: self.swap(a, a + 1, **kwargs) for a in range(lo, hi - 1)]
+        if i < j:
+            steps.append(lambda: self.apply_two_qudit_gate(gate, hi - 1, hi, **kwargs))
+        else:
+            steps.append(lambda: self.apply_two_qudit_gate(gate, hi, hi - 1, **kwargs))
+        steps += [lambda a=a: self.swap(a, a + 1, **kwargs) for a in range(hi - 2, lo - 1, -1)]
+        return steps
 
     def apply_layer(self, one_qudit: Optional[np.ndarray], pair_left: Sequence[int],
                     two_qudit: Optional[np.ndarray], **kwargs) -> None:

@@ -122,3 +122,65 @@ def test_one_qudit_gates_are_queued_and_ordered(cuda):
     state = np.moveaxis(np.tensordot(cn, state, axes=([2, 3], [2, 3])), [0, 1], [2, 3])
     state = one(state, u[0], 2)
     assert np.allclose(psi, state.reshape(-1), atol=2e-6)
+
+
+def test_disjoint_swap_chains_are_interleaved(cuda, monkeypatch):
+    """MPS.apply interleaves the SWAP chains of two-qudit operations on
+    disjoint site ranges (the k-th SWAP of each chain in one launch): the
+    state equals in-order application (apply_two_qudit_gate one by one, with
+    truncating SWAPs) with fewer launches, and without truncation the oracle's
+    state; overlapping ranges stay in order."""
+    from oracle.ref_mps import OracleMPS
+    n, d = 12, 2
+    rng = np.random.default_rng(21)
+    ops = []
+    for layer in range(4):
+        for q in range(n):
+            u1 = G.haar_random_matrix(1, 2, int(rng.integers(1 << 30)))
+            ops.append(MPSOperation(G.Node(np.asarray(u1)), q))
+        # disjoint long-range pairs (both orientations) and an adjacent one,
+        # then one whose range overlaps them
+        for a, b in ((0, 4), (9, 5), (10, 11), (3, 8)):
+            u = G.haar_random_matrix(2, 2, int(rng.integers(1 << 30)))
+            ops.append(MPSOperation(G.Node(np.asarray(u).reshape((2,) * 4)), (a, b)))
+
+    calls = []
+    orig = MPS._run_pair_group
+    monkeypatch.setattr(MPS, "_run_pair_group",
+                        lambda self, pairs, prec: (calls.append(len(pairs)), orig(self, pairs, prec)))
+
+    def in_order(kw):
+        m = MPS(n, d)
+        for op in ops:
+            if op.is_single_qudit_operation():
+                m.apply_one_qudit_gate(op.node(), op.qudit_indices[0])
+            else:
+                m.apply_two_qudit_gate(op.node(), *op.qudit_indices, **kw)
+                m._flush()
+        return m
+
+    kw = {"maxsvals": 6}
+    a = MPS(n, d)
+    a.apply(ops, **kw)
+    wa = a.wavefunction()
+    inter = list(calls)
+    calls.clear()
+    b = in_order(kw)
+    wb = b.wavefunction()
+    seq = list(calls)
+    assert list(a.bond_dimensions()) == list(b.bond_dimensions())
+    assert np.allclose(wa, wb, atol=1e-5)
+    assert sum(inter) == sum(seq)            # the same gates ...
+    assert len(inter) < len(seq)             # ... in fewer launches
+    assert max(inter) >= 3                   # the disjoint chains shared launches
+
+    a = MPS(n, d)
+    a.apply(ops)
+    o = OracleMPS(n, d)
+    for op in ops:
+        if op.is_single_qudit_operation():
+            o.apply_one_qudit_gate(np.asarray(op.tensor()), op.qudit_indices[0])
+        else:
+            o.apply_two_qudit_gate(np.asarray(op.tensor()), *op.qudit_indices)
+    assert np.allclose(a.wavefunction(), o.wavefunction(), atol=2e-6)
+    assert list(a.bond_dimensions()) == [int(s.shape[2]) for s in o.sites[:-1]]
