@@ -112,7 +112,8 @@ struct Aux {
     int rotated;          // some pair of this visit needs a rotation
     int col[TJ_W];        // physical column of each visit column (-1: zero padding)
     float diag[TJ_W];     // diagonal of G (squared column norms)
-    cf gam[TJ_W / 2];     // G[cP][cQ] of the 32 pairs of the next inner step
+    cf gam[TJ_W];         // G[cP][cQ] of the 32 pairs of the next inner step (the ring
+                          // visit double-buffers it: [step parity][pair])
     float cmax;           // largest squared cosine of the visit's pairs
 };
 constexpr size_t TJ_SMEM = TJ_AUX + sizeof(Aux) + 1024;
@@ -436,20 +437,163 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
         __syncthreads();
     }
     const bool work = ax.rotated != 0;
-    const int nsteps = full ? TJ_W - 1 : TJ_BC;
+    const int nsteps = TJ_W - 1;           // the full visit's steps
     int rsteps = 0, rpairs = 0;
-    if (work) {
+    if (work && !full) {
+        // Ring visit (the 32 x 32 inter-block pairs), 2 x 2 blocks: step s
+        // pairs index k with 32 + (k + s) % 32 on both sides of G, so row
+        // pair i and column pair k span a 2 x 2 block of G that the step
+        // changes as R_i^H B R_k.  Thread (warp w, lane k) holds the blocks
+        // of column pair k and row pairs i = w + 8h (h < 4): PP = G[i][k],
+        // PQ = G[i][q_k], QP = G[q_i][k], QQ = G[q_i][q_k] -- all of a step's
+        // arithmetic on G is local.  Between steps the Q columns move one
+        // lane down (shuffles) and the Q rows one row pair down (row pair
+        // i + 1's, through a double-buffered shared array in the H area),
+        // so a step has one barrier.  E (Y <- Y + Y E) keeps the column
+        // layout of the full visit: rows w + 8h (h < 8), columns k and q_k.
+        const int cP = lane;
+        int cQ = TJ_BC + lane;
+        cf bPP[4], bPQ[4], bQP[4], bQQ[4], eP[8], eQ[8];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const int i = warp + 8 * h;
+            bPP[h] = G[gidx(i, cP)];
+            bPQ[h] = G[gidx(i, cQ)];
+            bQP[h] = G[gidx(TJ_BC + i, cP)];
+            bQQ[h] = G[gidx(TJ_BC + i, cQ)];
+        }
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+            eP[h] = cmake(0.f, 0.f);
+            eQ[h] = cmake(0.f, 0.f);
+        }
+        cf* const xq = reinterpret_cast<cf*>(smem + TJ_HOFF);   // [2][32 row pairs][32][2]
+        {
+            // gamma of pair k = G[k][q_k] = PQ of row pair k (warp k % 8)
+            cf v = cmake(0.f, 0.f);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const float m = (warp + 8 * h == cP) ? 1.f : 0.f;
+                v.x = fmaf(m, bPQ[h].x, v.x);
+                v.y = fmaf(m, bPQ[h].y, v.y);
+            }
+            if (warp == (cP & 7)) ax.gam[lane] = v;
+        }
+        float dP = ax.diag[cP], dQ = ax.diag[cQ];
+        __syncthreads();
+        for (int s = 0; s < TJ_BC; ++s) {
+            const int b = s & 1;
+            if (s > 0) {
+                // this step's Q rows: row pair i + 1's of the previous step
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int i1 = (warp + 8 * h + 1) & 31;
+                    const float4 q = *reinterpret_cast<const float4*>(
+                        xq + ((size_t)((b ^ 1) * 32 + i1) * 32 + lane) * 2);
+                    bQP[h] = cmake(q.x, q.y);
+                    bQQ[h] = cmake(q.z, q.w);
+                }
+            }
+            float tp = 0.f, na = 0.f, nb = 0.f;
+            cf sg = cmake(0.f, 0.f);
+            bool rot;
+            {
+                const float a = dP, bb = dQ;
+                const cf gam = ax.gam[(b * 32) + lane];
+                rot = pair_cos2(gam, cabs2(gam), a, bb) > tol2;
+                if (rot) {
+                    const Rot r = make_rot(a, bb, gam);
+                    tp = r.tp;
+                    sg = r.sigma;
+                    na = a - r.dn;
+                    nb = bb + r.dn;
+                }
+            }
+            const unsigned rmask = __ballot_sync(0xffffffffu, rot);
+            if (rmask) {
+                ++rsteps;
+                rpairs += __popc(rmask);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    // the rotation of row pair i = w + 8h, from lane i
+                    const int i = warp + 8 * h;
+                    const float tpi = __shfl_sync(0xffffffffu, tp, i);
+                    const cf sgi = cmake(__shfl_sync(0xffffffffu, sg.x, i),
+                                         -__shfl_sync(0xffffffffu, sg.y, i));   // conj
+                    rotate_cols(bPP[h], bPQ[h], tp, sg);
+                    rotate_cols(bQP[h], bQQ[h], tp, sg);
+                    rotate_cols(bPP[h], bQP[h], tpi, sgi);
+                    rotate_cols(bPQ[h], bQQ[h], tpi, sgi);
+                }
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    const int r = warp + 8 * h;
+                    rotate_cols(eP[h], eQ[h], tp, sg);
+                    const float mp = r == cP ? 1.f : 0.f, mq = r == cQ ? 1.f : 0.f;
+                    eP[h].x = fmaf(-mp, tp, fmaf(-mq, sg.x, eP[h].x));
+                    eP[h].y = fmaf(-mq, sg.y, eP[h].y);
+                    eQ[h].x = fmaf(mp, sg.x, fmaf(-mq, tp, eQ[h].x));
+                    eQ[h].y = fmaf(-mp, sg.y, eQ[h].y);
+                }
+                if (rot) {
+                    dP = na;
+                    dQ = nb;
+                }
+            }
+            if (s + 1 < TJ_BC) {
+                // the Q columns move to the lane of their next pair
+                const int src = (lane + 1) & 31;
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    bPQ[h] = shfl_cf(bPQ[h], src);
+                    bQQ[h] = shfl_cf(bQQ[h], src);
+                }
+#pragma unroll
+                for (int h = 0; h < 8; ++h) eQ[h] = shfl_cf(eQ[h], src);
+                cQ = __shfl_sync(0xffffffffu, cQ, src);
+                dQ = __shfl_sync(0xffffffffu, dQ, src);
+                // the Q rows go to the row pair below through shared memory
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int i = warp + 8 * h;
+                    *reinterpret_cast<float4*>(xq + ((size_t)(b * 32 + i) * 32 + lane) * 2) =
+                        make_float4(bQP[h].x, bQP[h].y, bQQ[h].x, bQQ[h].y);
+                }
+                // the next step's gamma of pair k: PQ of row pair k
+                cf v = cmake(0.f, 0.f);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const float m = (warp + 8 * h == cP) ? 1.f : 0.f;
+                    v.x = fmaf(m, bPQ[h].x, v.x);
+                    v.y = fmaf(m, bPQ[h].y, v.y);
+                }
+                if (warp == (cP & 7)) ax.gam[((b ^ 1) * 32) + lane] = v;
+            }
+            __syncthreads();
+        }
+        if (warp == 0) {
+            ax.diag[cP] = dP;
+            ax.diag[cQ] = dQ;
+        }
+        __syncthreads();                  // the diagonal is read below
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+            const int r = warp + 8 * h;
+            E[r * TJ_W + cP] = eP[h];
+            E[r * TJ_W + cQ] = eQ[h];
+        }
+    } else if (work) {
+        // Full visit (all 2016 pairs of the 64 columns, 63 steps).
         // Register-resident: warp w holds rows w, w + 8, ... of G and E, lane
         // k the two columns of pair k (visit columns cP, cQ).  The column
         // rotations of both passes are then local; between the passes H goes
         // through shared memory conjugate-transposed, and between the steps
-        // the columns move to the lanes of their next pairs by shuffles: the
-        // ring's q-columns shift by one lane, the full visit's 63 steps are
-        // the circle method (cP of lane 0 fixed, the other 63 columns moving
+        // the columns move to the lanes of their next pairs by shuffles in the
+        // circle method (cP of lane 0 fixed, the other 63 columns moving
         // along t1 -> t2 -> ... -> t31 -> b31 -> ... -> b0 -> t1).  The angle
         // inputs of a step, diag and gamma = G[cP][cQ], come from the warps
         // holding those rows, through the small arrays.
-        int cP = lane, cQ = full ? TJ_W - 1 - lane : TJ_BC + lane;
+        int cP = lane, cQ = TJ_W - 1 - lane;
         cf gP[8], gQ[8], eP[8], eQ[8];
 #pragma unroll
         for (int h = 0; h < 8; ++h) {
@@ -524,27 +668,16 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             }
             if (s + 1 < nsteps) {
                 // the columns move to the lanes of the next step's pairs
-                if (!full) {
-                    const int src = (lane + 1) & 31;
 #pragma unroll
-                    for (int h = 0; h < 8; ++h) {
-                        gQ[h] = shfl_cf(gQ[h], src);
-                        eQ[h] = shfl_cf(eQ[h], src);
-                    }
-                    cQ = __shfl_sync(0xffffffffu, cQ, src);
-                    dQ = __shfl_sync(0xffffffffu, dQ, src);
-                } else {
-#pragma unroll
-                    for (int h = 0; h < 8; ++h) {
-                        circle_move(gP[h], gQ[h], lane);
-                        circle_move(eP[h], eQ[h], lane);
-                    }
-                    circle_move_idx(cP, cQ, lane);
-                    cf d = cmake(dP, dQ);
-                    circle_move_pair(d, lane);
-                    dP = d.x;
-                    dQ = d.y;
+                for (int h = 0; h < 8; ++h) {
+                    circle_move(gP[h], gQ[h], lane);
+                    circle_move(eP[h], eQ[h], lane);
                 }
+                circle_move_idx(cP, cQ, lane);
+                cf d = cmake(dP, dQ);
+                circle_move_pair(d, lane);
+                dP = d.x;
+                dQ = d.y;
                 publish_gamma(gQ, warp, cP, ax.gam + lane);
             }
             __syncthreads();
