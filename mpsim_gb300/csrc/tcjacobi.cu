@@ -444,19 +444,20 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
         // pairs index k with 32 + (k + s) % 32 on both sides of G, so row
         // pair i and column pair k span a 2 x 2 block of G that the step
         // changes as R_i^H B R_k.  Thread (warp w, lane k) holds the blocks
-        // of column pair k and row pairs i = w + 8h (h < 4): PP = G[i][k],
+        // of column pair k and row pairs i = 4w + h (h < 4): PP = G[i][k],
         // PQ = G[i][q_k], QP = G[q_i][k], QQ = G[q_i][q_k] -- all of a step's
         // arithmetic on G is local.  Between steps the Q columns move one
-        // lane down (shuffles) and the Q rows one row pair down (row pair
-        // i + 1's, through a double-buffered shared array in the H area),
-        // so a step has one barrier.  E (Y <- Y + Y E) keeps the column
-        // layout of the full visit: rows w + 8h (h < 8), columns k and q_k.
+        // lane down (shuffles) and the Q rows one row pair down: row pair
+        // i + 1's, in the same thread but for h = 3, which takes row pair
+        // 4(w + 1)'s through a double-buffered shared array in the H area; a
+        // step has one barrier.  E (Y <- Y + Y E) keeps the column layout of
+        // the full visit: rows w + 8h (h < 8), columns k and q_k.
         const int cP = lane;
         int cQ = TJ_BC + lane;
         cf bPP[4], bPQ[4], bQP[4], bQQ[4], eP[8], eQ[8];
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
-            const int i = warp + 8 * h;
+            const int i = 4 * warp + h;
             bPP[h] = G[gidx(i, cP)];
             bPQ[h] = G[gidx(i, cQ)];
             bQP[h] = G[gidx(TJ_BC + i, cP)];
@@ -467,32 +468,27 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             eP[h] = cmake(0.f, 0.f);
             eQ[h] = cmake(0.f, 0.f);
         }
-        cf* const xq = reinterpret_cast<cf*>(smem + TJ_HOFF);   // [2][32 row pairs][32][2]
+        float4* const xq = reinterpret_cast<float4*>(smem + TJ_HOFF);   // [2][8 warps][32]
         {
-            // gamma of pair k = G[k][q_k] = PQ of row pair k (warp k % 8)
+            // gamma of pair k = G[k][q_k] = PQ of row pair k (warp k / 4)
             cf v = cmake(0.f, 0.f);
 #pragma unroll
             for (int h = 0; h < 4; ++h) {
-                const float m = (warp + 8 * h == cP) ? 1.f : 0.f;
+                const float m = (4 * warp + h == cP) ? 1.f : 0.f;
                 v.x = fmaf(m, bPQ[h].x, v.x);
                 v.y = fmaf(m, bPQ[h].y, v.y);
             }
-            if (warp == (cP & 7)) ax.gam[lane] = v;
+            if (warp == (cP >> 2)) ax.gam[lane] = v;
         }
         float dP = ax.diag[cP], dQ = ax.diag[cQ];
         __syncthreads();
         for (int s = 0; s < TJ_BC; ++s) {
             const int b = s & 1;
             if (s > 0) {
-                // this step's Q rows: row pair i + 1's of the previous step
-#pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    const int i1 = (warp + 8 * h + 1) & 31;
-                    const float4 q = *reinterpret_cast<const float4*>(
-                        xq + ((size_t)((b ^ 1) * 32 + i1) * 32 + lane) * 2);
-                    bQP[h] = cmake(q.x, q.y);
-                    bQQ[h] = cmake(q.z, q.w);
-                }
+                // the last row pair's Q row: row pair 4(w + 1)'s of the previous step
+                const float4 q = xq[((b ^ 1) * 8 + ((warp + 1) & 7)) * 32 + lane];
+                bQP[3] = cmake(q.x, q.y);
+                bQQ[3] = cmake(q.z, q.w);
             }
             float tp = 0.f, na = 0.f, nb = 0.f;
             cf sg = cmake(0.f, 0.f);
@@ -515,8 +511,8 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                 rpairs += __popc(rmask);
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
-                    // the rotation of row pair i = w + 8h, from lane i
-                    const int i = warp + 8 * h;
+                    // the rotation of row pair i = 4w + h, from lane i
+                    const int i = 4 * warp + h;
                     const float tpi = __shfl_sync(0xffffffffu, tp, i);
                     const cf sgi = cmake(__shfl_sync(0xffffffffu, sg.x, i),
                                          -__shfl_sync(0xffffffffu, sg.y, i));   // conj
@@ -552,22 +548,23 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                 for (int h = 0; h < 8; ++h) eQ[h] = shfl_cf(eQ[h], src);
                 cQ = __shfl_sync(0xffffffffu, cQ, src);
                 dQ = __shfl_sync(0xffffffffu, dQ, src);
-                // the Q rows go to the row pair below through shared memory
+                // the Q rows move one row pair down: row pair 4w's to the
+                // warp above through shared memory, the others in the thread
+                xq[(b * 8 + warp) * 32 + lane] = make_float4(bQP[0].x, bQP[0].y, bQQ[0].x, bQQ[0].y);
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    const int i = warp + 8 * h;
-                    *reinterpret_cast<float4*>(xq + ((size_t)(b * 32 + i) * 32 + lane) * 2) =
-                        make_float4(bQP[h].x, bQP[h].y, bQQ[h].x, bQQ[h].y);
+                for (int h = 0; h < 3; ++h) {
+                    bQP[h] = bQP[h + 1];
+                    bQQ[h] = bQQ[h + 1];
                 }
                 // the next step's gamma of pair k: PQ of row pair k
                 cf v = cmake(0.f, 0.f);
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
-                    const float m = (warp + 8 * h == cP) ? 1.f : 0.f;
+                    const float m = (4 * warp + h == cP) ? 1.f : 0.f;
                     v.x = fmaf(m, bPQ[h].x, v.x);
                     v.y = fmaf(m, bPQ[h].y, v.y);
                 }
-                if (warp == (cP & 7)) ax.gam[((b ^ 1) * 32) + lane] = v;
+                if (warp == (cP >> 2)) ax.gam[((b ^ 1) * 32) + lane] = v;
             }
             __syncthreads();
         }
