@@ -688,6 +688,8 @@ def run_case(args):
       layer256        one mps_apply_2q_batch call: 32 jobs of theta 512 x 512
                       (random sites, Haar gates), plain form
       layer256_mixed  the same call in MPS_PRECISION_MIXED
+      batched256      the same with 512 jobs (the batched form), plain
+      batched256_mixed  ... and in MPS_PRECISION_MIXED
       onequbit256     one mps_apply_1q_batch over 64 sites of (256, 2, 256):
                       HBM-bound, 2 x 64 x 1 MiB moved
       norm256         MPS.norm of a 64-site chi=256 state (the overlap sweep)
@@ -713,8 +715,8 @@ def run_case(args):
         return torch.from_numpy((t * scale).astype(np.complex64)).to(dev)
 
     keep = []
-    if args.case in ("layer256", "layer256_mixed"):
-        njobs = 32
+    if args.case in ("layer256", "layer256_mixed", "batched256", "batched256_mixed"):
+        njobs = 512 if args.case.startswith("batched") else 32
         A, B = rand_sites(njobs, chi, chi, 1.0 / chi), rand_sites(njobs, chi, chi, 1.0)
         G = torch.from_numpy(np.stack([haar_random_matrix(2, d, 100 + q) for q in range(njobs)])
                              .astype(np.complex64)).to(dev)
@@ -730,7 +732,7 @@ def run_case(args):
         nbytes = lib.mps_2q_workspace_bytes_mixed(njobs, 2 * chi, 2 * chi, d)
         ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
         params = _native.SvdParams()
-        params.precision = (_native.PRECISION_MIXED if args.case == "layer256_mixed"
+        params.precision = (_native.PRECISION_MIXED if args.case.endswith("_mixed")
                             else _native.PRECISION_PLAIN)
 
         def once():
@@ -802,9 +804,9 @@ def run_case(args):
     if unit.startswith("GB/s"):
         line["frac_of_hbm_copy"] = line["achieved"] / peaks["hbm_gbs"]
         line["peak_source"] = f"hbm_gbs ({kind})"
-    if args.case in ("layer256", "layer256_mixed"):
+    if args.case in ("layer256", "layer256_mixed", "batched256", "batched256_mixed"):
         line["sweeps"] = int(params.sweeps_out)
-    if args.case == "layer256_mixed":
+    if args.case.endswith("_mixed"):
         # cycles of the tensor-core visits per step (one more call, counters
         # reset before it): Gram, rotations on G, update; and the visit count
         cyc = (ctypes.c_ulonglong * 10)()
@@ -837,7 +839,8 @@ def main():
     ap.add_argument("--ncircuits", type=int, default=0)
     ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
     ap.add_argument("--case", default=None,
-                    choices=["layer256", "layer256_mixed", "onequbit256", "norm256", "tcgemm"],
+                    choices=["layer256", "layer256_mixed", "batched256", "batched256_mixed",
+                             "onequbit256", "norm256", "tcgemm"],
                     help="time one kernel family on a chi=256 case (for profiling)")
     args = ap.parse_args()
 
