@@ -94,6 +94,12 @@ constexpr uint32_t TJ_MGRP = 8192;                  // one 64-real M-group of an
 constexpr uint32_t TJ_AUX = 2 * TJ_GTILE;           // 96 KB: small arrays
 constexpr uint32_t TJ_TMEM_COLS = 128;              // two 64-column Gram accumulators
 constexpr int TJ_WAIT_LIMIT = 1 << 14;
+// Inside a visit that has work (some pair over the tolerance by the FP64
+// test), every pair whose squared cosine exceeds kInnerTol2 tol^2 rotates:
+// pairs that the visit's rounding would leave just over the tolerance are
+// settled now instead of bringing their blocks back a sweep later (per job
+// about one sweep fewer; the convergence record keeps the FP64 test at tol).
+constexpr float kInnerTol2 = 0.25f;
 static_assert(TJ_EOFF + TJ_GBUF <= TJ_AUX, "E overlaps the small arrays");
 static_assert(TJ_AOFF + 3 * TJ_PIECE <= TJ_AUX, "the update's A tiles overlap the small arrays");
 
@@ -496,7 +502,7 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             {
                 const float a = dP, bb = dQ;
                 const cf gam = ax.gam[(b * 32) + lane];
-                rot = pair_cos2(gam, cabs2(gam), a, bb) > tol2;
+                rot = pair_cos2(gam, cabs2(gam), a, bb) > kInnerTol2 * tol2;
                 if (rot) {
                     const Rot r = make_rot(a, bb, gam);
                     tp = r.tp;
@@ -614,8 +620,8 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
             {
                 const float a = dP, b = dQ;
                 const cf gam = ax.gam[lane];
-                // per-step rotation decision in FP32 (the SIMT form's test)
-                rot = pair_cos2(gam, cabs2(gam), a, b) > tol2;
+                // per-step rotation decision in FP32 (kInnerTol2 above)
+                rot = pair_cos2(gam, cabs2(gam), a, b) > kInnerTol2 * tol2;
                 if (rot) {
                     const Rot r = make_rot(a, b, gam);
                     tp = r.tp;
