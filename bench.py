@@ -837,7 +837,7 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncircuits", type=int, default=0)
-    ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--precision", default="plain", choices=["plain", "mixed", "auto"])
     ap.add_argument("--case", default=None,
                     choices=["layer256", "layer256_mixed", "batched256", "batched256_mixed",
                              "onequbit256", "norm256", "tcgemm"],
@@ -1041,9 +1041,12 @@ def main():
             "data": "synthetic (seeded Haar gates)",
             "config": {"workload": args.workload, "nqudits": circ.nqudits, "depth": circ.depth,
                        "maxsvals": maxs, "two_qudit_gates_per_step": ngates,
-                       "precision": ("plain complex64, FP32 SIMT" if args.precision == "plain" else
-                                     "mixed: tcgen05 split-bf16 block Jacobi for left-canonical "
-                                     "gates of 64+ columns, FP32 SIMT elsewhere"),
+                       "precision": {"plain": "plain complex64, FP32 SIMT",
+                                     "mixed": "mixed: tcgen05 split-bf16 block Jacobi for "
+                                              "left-canonical gates of 64+ columns, FP32 SIMT "
+                                              "elsewhere",
+                                     "auto": "auto: per call, the form the tuning table "
+                                             "measured faster"}[args.precision],
                        "parallelism": f"replicas x{world}",
                        "l2": "256 MiB buffer written at the start of every step"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,

@@ -35,7 +35,13 @@ from . import _native
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE_PATH = os.path.join(HERE, "tuning", "gb300.json")
-BUCKETS = (8, 64, 1 << 30)
+# Batch-size buckets of the table: a call of njobs jobs takes the entry of the
+# smallest bucket >= njobs, which is measured at the smallest batch the bucket
+# covers (the previous bound + 1).  The mixed form's advantage grows with the
+# batch (a visit's latency bounds it, the plain form is bound by its work), so
+# a bucket takes the mixed form only where it wins for every batch it covers.
+BUCKETS = (8, 16, 32, 64, 128, 256, 1 << 30)
+TUNE_BATCHES = (1,) + tuple(b + 1 for b in BUCKETS[:-1])
 DEFAULT = {"lq_off": 0, "block_request": 0, "precision": "plain"}
 
 _table = None
@@ -139,7 +145,7 @@ def _time(lib, keep, S, njobs, m, n, d, cand, reps, ws):
     return float(np.median(times)), S.cpu().numpy().copy()
 
 
-def tune(shapes, njobs_list=(8, 32, 512), reps: int = 3, device=None, log=print) -> Dict:
+def tune(shapes, njobs_list=TUNE_BATCHES, reps: int = 3, device=None, log=print) -> Dict:
     """Times every candidate for each (chi_l, chi_m, chi_r, d) shape and batch
     size; returns {key: {settings..., "ms": {candidate: ms}}}."""
     import torch

@@ -9,9 +9,12 @@ from mpsim_gb300 import autotune as A
 
 
 def test_buckets_and_keys():
-    assert A.bucket(1) == 8 and A.bucket(8) == 8 and A.bucket(9) == 64 and A.bucket(5000) > 64
-    assert A.key(512, 512, 2, 32) == "d2_m512_n512_b64"
+    assert A.bucket(1) == 8 and A.bucket(8) == 8 and A.bucket(9) == 16 and A.bucket(5000) > 256
+    assert A.key(512, 512, 2, 32) == "d2_m512_n512_b32"
     assert A.key(512, 512, 2, 4) != A.key(512, 512, 2, 400)
+    # each bucket is tuned at the smallest batch it covers
+    assert [A.bucket(n) for n in A.TUNE_BATCHES] == list(A.BUCKETS)
+    assert all(A.bucket(n - 1) != A.bucket(n) for n in A.TUNE_BATCHES[1:])
 
 
 def test_lookup_defaults_and_override():
