@@ -221,3 +221,47 @@ def test_status_words_checked_after_the_call():
         MPS._check_status(me, block=True)
     assert ei.value.code == _native.MPS_ERR_NONFINITE
     assert me._status_pending == []
+
+
+def test_wide_split_compression_keeps_u_and_s(monkeypatch):
+    """_wide_left_svd's column-block compression (the host logic of
+    from_wavefunction's long splits), with the device SVD and GEMM replaced by
+    NumPy: every level keeps mat mat^H, so U and S are those of mat, and the
+    remainder U^H mat rebuilds it.  Covers several levels, a ragged last
+    block and a matrix within the kernel's length."""
+    import torch
+    from mpsim_gb300 import core
+
+    def fake_batch(device, stream, mats, left_canonical, on_unconverged="raise"):
+        a = mats.numpy().astype(np.complex128)
+        u, s, vh = np.linalg.svd(a, full_matrices=False)
+        left = u if left_canonical else u * s[:, None, :]
+        right = s[:, :, None] * vh if left_canonical else vh
+        t = lambda x: torch.from_numpy(x.astype(np.complex64))
+        return t(left), t(right), torch.from_numpy(s.astype(np.float32))
+
+    def fake_cgemm(lib, stream, m, n, k, a, a_off, sam, sak, conj_a, b, b_off, sbk, sbn, conj_b,
+                   c, c_off, scm, scn, batch=1, bsa=0, bsb=0, bsc=0):
+        fa, fb = a.reshape(-1).numpy(), b.reshape(-1).numpy()
+        A = fa[a_off + np.arange(m)[:, None] * sam + np.arange(k)[None, :] * sak]
+        B = fb[b_off + np.arange(k)[:, None] * sbk + np.arange(n)[None, :] * sbn]
+        C = (np.conj(A) if conj_a else A) @ (np.conj(B) if conj_b else B)
+        c.reshape(-1)[c_off + (np.arange(m)[:, None] * scm + np.arange(n)[None, :] * scn).ravel()] = \
+            torch.from_numpy(C.astype(np.complex64).ravel())
+
+    monkeypatch.setattr(core, "_given_svd_batch", fake_batch)
+    monkeypatch.setattr(core, "_cgemm", fake_cgemm)
+    monkeypatch.setattr(core._native, "load", lambda: None)
+    rng = np.random.default_rng(3)
+    for m, n in ((2, 9000), (40, 5000), (700, 2100), (1200, 4000), (64, 1500)):
+        mat = (rng.normal(size=(m, n)) + 1j * rng.normal(size=(m, n))).astype(np.complex64)
+        u, rest = core._wide_left_svd("cpu", None, torch.from_numpy(mat))
+        u, rest = u.numpy().astype(np.complex128), rest.numpy().astype(np.complex128)
+        assert u.shape == (m, m) and rest.shape == (m, n)
+        assert np.allclose(u.conj().T @ u, np.eye(m), atol=1e-4)
+        assert np.allclose(u @ rest, mat, atol=1e-3 * np.abs(mat).max())
+        s_ref = np.linalg.svd(mat.astype(np.complex128), compute_uv=False)
+        s_got = np.sort(np.linalg.norm(rest, axis=1))[::-1]
+        assert np.allclose(s_got, s_ref, rtol=1e-4)
+    with pytest.raises(NotImplementedError):
+        core._wide_left_svd("cpu", None, torch.zeros((core.MAX_SVD_LENGTH, 4000), dtype=torch.complex64))
