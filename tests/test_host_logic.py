@@ -265,3 +265,65 @@ def test_wide_split_compression_keeps_u_and_s(monkeypatch):
         assert np.allclose(s_got, s_ref, rtol=1e-4)
     with pytest.raises(NotImplementedError):
         core._wide_left_svd("cpu", None, torch.zeros((core.MAX_SVD_LENGTH, 4000), dtype=torch.complex64))
+
+
+def test_apply_interleaves_disjoint_swap_chains_exactly():
+    """MPS.apply's scheduling, on a recording stand-in for the state: the
+    adjacent steps it issues (SWAP chains of non-adjacent gates interleaved
+    across disjoint site ranges, one-qudit gates and overlapping ranges ending
+    a group) applied to a dense state vector give the in-order result, and the
+    chains of disjoint gates do interleave."""
+    from mpsim_gb300.gates import gate_tensor
+
+    n = 7
+    rng = np.random.default_rng(11)
+
+    class Rec:
+        track_norms = False
+
+        def __init__(self):
+            self.steps = []
+
+        def _check_two_qudit(self, gate, i, j):
+            assert 0 <= i < n and 0 <= j < n and i != j
+
+        def _two_qudit_steps(self, gate, i, j, kw):
+            return MPS._two_qudit_steps(self, gate, i, j, kw)
+
+        def swap(self, a, b, **kw):
+            self.steps.append(("2", np.asarray(gate_tensor(G.swap())), a, b))
+
+        def apply_two_qudit_gate(self, gate, i, j, **kw):
+            assert abs(i - j) == 1
+            self.steps.append(("2", np.asarray(gate_tensor(gate)), i, j))
+
+        def apply_one_qudit_gate(self, gate, i, **kw):
+            self.steps.append(("1", np.asarray(gate_tensor(gate)), i))
+
+    def dense(seq):
+        psi = np.zeros((2,) * n, complex)
+        psi[(0,) * n] = 1.0
+        for st in seq:
+            if st[0] == "1":
+                psi = np.moveaxis(np.tensordot(st[1].reshape(2, 2), psi, axes=([1], [st[2]])), 0, st[2])
+            else:
+                g, i, j = st[1].reshape(2, 2, 2, 2), st[2], st[3]
+                psi = np.moveaxis(np.tensordot(g, psi, axes=([2, 3], [i, j])), [0, 1], [i, j])
+        return psi.reshape(-1)
+
+    ops, ref = [], []
+    for layer in range(3):
+        for q in range(n):
+            u = G.haar_random_matrix(1, 2, int(rng.integers(1 << 30)))
+            ops.append(MPSOperation(G.Node(np.asarray(u)), q))
+            ref.append(("1", np.asarray(u), q))
+        for a, b in ((0, 3), (6, 4), (2, 5)):              # the last overlaps both
+            u = np.asarray(G.haar_random_matrix(2, 2, int(rng.integers(1 << 30)))).reshape((2,) * 4)
+            ops.append(MPSOperation(G.Node(u), (a, b)))
+            ref.append(("2", u, a, b))
+    rec = Rec()
+    MPS.apply(rec, ops)
+    assert np.allclose(dense(rec.steps), dense(ref), atol=1e-10)
+    # the first steps of the (0, 3) and (6, 4) chains sit next to each other
+    two = [s for s in rec.steps if s[0] == "2"]
+    assert (two[0][2], two[0][3]) == (0, 1) and (two[1][2], two[1][3]) == (4, 5)
