@@ -554,8 +554,9 @@ __device__ __forceinline__ bool visit(const TwoQGeom& g, int j, int I, int J, bo
                 for (int h = 0; h < 8; ++h) eQ[h] = shfl_cf(eQ[h], src);
                 cQ = __shfl_sync(0xffffffffu, cQ, src);
                 dQ = __shfl_sync(0xffffffffu, dQ, src);
-                // the Q rows move one row pair down: row pair 4w's to the
-                // warp above through shared memory, the others in the thread
+                // the Q rows move one row pair down: row pair 4w's goes to
+                // warp w - 1 (for its row pair 4w - 1) through shared memory,
+                // the others within the thread
                 xq[(b * 8 + warp) * 32 + lane] = make_float4(bQP[0].x, bQP[0].y, bQQ[0].x, bQQ[0].y);
 #pragma unroll
                 for (int h = 0; h < 3; ++h) {
