@@ -726,6 +726,11 @@ presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2, int b
     const int m = jobs[j].chi_l * g.d, n = jobs[j].chi_r * g.d;
     const int C = min(m, n);
     if (C < 2) return;
+    // The tensor-core sweeps keep their columns in place: measured, their jobs
+    // converge about a sweep sooner unsorted (the LQ factor's own column order,
+    // and blocks that keep their columns keep their visits skippable), while
+    // the SIMT sweeps gain from the sort.
+    if (g.tc_mode && tc_job(m, n, jobs[j].keep_left_canonical)) return;
     const int tid = threadIdx.x;
     const float* cn = g.cnrm + (size_t)j * g.cslot;
     for (int i = tid; i < npow2; i += PRESORT_T) {
@@ -756,7 +761,6 @@ presort_kernel(const mps_2q_job* __restrict__ jobs, TwoQGeom g, int npow2, int b
             __syncthreads();
         }
     }
-    if (g.tc_mode && tc_job(m, n, jobs[j].keep_left_canonical)) bc = 32;   // tensor-core blocks
     if (g.vstamp) {
         // a block whose set of columns changes counts as changed (its pairs
         // are not the ones last checked); moves inside a block do not
