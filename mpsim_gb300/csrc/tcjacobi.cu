@@ -18,9 +18,10 @@
 // planes of a 32-job chi=256 call, 96 MB, mostly stay in L2).
 //
 // The C columns are split into blocks of 32.  A sweep visits every pair of
-// blocks once (circle-method rounds over the norm-sorted column order, as in
-// the SIMT form).  One visit of blocks (I, J), Y = [X_I X_J] (L x 64 complex),
-// by one 256-thread CTA:
+// blocks once (circle-method rounds, as in the SIMT form, over the L factor's
+// own column order: unlike the SIMT form's, these jobs are not re-sorted by
+// norm before each sweep, which measured a sweep fewer).  One visit of blocks
+// (I, J), Y = [X_I X_J] (L x 64 complex), by one 256-thread CTA:
 //   1. Gram:     G = Y^H Y (64 x 64 complex) on the tensor cores.  Real form:
 //                rows 0..63 of the operand tile are the columns of Y as
 //                interleaved (re, im) vectors of length 2L, rows 64..127 are
@@ -39,17 +40,20 @@
 //   2. Convergence test and rotations on G.  The off-diagonal test runs
 //                first, in FP64 on the fresh Gram: a visit none of whose
 //                pairs has |G_pq|^2 > tol^2 G_pp G_qq changes nothing and
-//                skips the rest.  Otherwise two-sided Jacobi on G in shared
-//                memory, 32 disjoint pairs per step (the 32 x 32 inter-block
-//                pairs in 32 steps, or all 2016 pairs in 63 steps on a block's
-//                first visit of a sweep), accumulating E = Q - I.  Every warp
+//                skips the rest.  Otherwise two-sided Jacobi on G held in
+//                registers, 32 disjoint pairs per step (the 32 x 32
+//                inter-block pairs in 32 steps, or all 2016 pairs in 63 steps
+//                on a block's first visit of a sweep), accumulating E = Q - I;
+//                every pair over kInnerTol2 tol^2 rotates.  Every warp
 //                computes the 32 rotations of a step (lane k: pair k, the FP32
 //                parameters of rot.cuh), so a step where no pair rotates is
-//                skipped by all warps alike, without a barrier.  G' = R^H G R
-//                in two passes with the same thread layout (lane k: pair k's
-//                two columns, warp w: rows w, w + 8, ...): H = G R written
-//                conjugate-transposed, then G' = H^H R (G is Hermitian); E
-//                takes R in the second pass.
+//                skipped by all warps alike.  Ring visits hold G as 2 x 2
+//                blocks (row pair x column pair) and apply R^H B R in the
+//                thread, one barrier a step; full visits hold rows w, w + 8,
+//                ... and lane k's two columns and take G' = R^H G R in two
+//                passes (H = G R written conjugate-transposed, then G' = H^H R;
+//                G is Hermitian), two barriers a step.  E takes R with the
+//                column layout in both.
 //   3. Update:   Y <- Y + Y E, skipped when the visit rotated nothing.  Per
 //                64 rows, the tensor cores form D1 = Y Re E and D2 = Y Im E
 //                from the rows' piece tiles read as an MN-major A operand
@@ -62,14 +66,16 @@
 //                is small once the rotations are (accumulating Y Q in full
 //                shrank every singular value by ~5e-5 over a chi=256 SVD).
 //                The piece products are issued smallest first.
-// The new squared column norms (the diagonal of Q^H G Q) go to cnrm for the
-// next sweep's sort.
+// The new squared column norms (the diagonal of Q^H G Q) go to cnrm, the
+// column-norm record the SIMT form sorts by.
 //
 // Shared memory (96 KB + the small arrays: two CTAs per SM):
 //   [0, 96K)   step 1: two tile buffers, each three 16 KB piece tiles
 //              (128 rows x 128 B, 128-byte swizzle)
-//   [0, 32K)   step 2: G (64 x 64 complex, columns XOR-swizzled by the row)
-//   [32K, 64K) step 2: H^H, the first pass's output (same layout)
+//   [0, 32K)   step 2: G (64 x 64 complex, columns XOR-swizzled by the row),
+//              read into registers at the start
+//   [32K, 64K) step 2: H^H, the first pass's output (full visits, same
+//              layout); the ring visits' Q-row exchange (8 KB)
 //   [64K, 96K) step 2: E = Q - I (64 x 64 complex, row-major)
 //   [0, 48K)   step 3: the three B-operand pieces of E (16 KB each)
 //   [48K, 96K) step 3: the three A piece tiles of 64 rows (two 8 KB M-groups
