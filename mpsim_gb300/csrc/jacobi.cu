@@ -713,7 +713,8 @@ __global__ void count_simt_jobs_kernel(const mps_2q_job* __restrict__ jobs, int 
 // (de Rijk's ordering), which cuts the sweep count.  The columns stay where
 // they are; presort_kernel sorts the squared norms the previous sweep's visits
 // left in cnrm (theta_norm_kernel's before the first sweep) and rewrites the
-// job's column map.  Converged jobs keep theirs.
+// job's column map.  Converged jobs keep theirs, and so do the tensor-core
+// jobs of a mixed call (see below).
 constexpr int PRESORT_T = 512;
 
 __global__ void __launch_bounds__(PRESORT_T)
